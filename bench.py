@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Benchmark: elements/s assembled into CSR (K, M and the load vector), Q1 hexahedra.
+
+Workload (one step): the perturbed 128^3 Q1-hex unit cube (2,097,152 elements,
+2,146,689 nodes; interior nodes moved by a seeded U(-0.2h, 0.2h) per coordinate),
+per-element diffusivity k_e = exp(N(0,1)), 2x2x2 Gauss quadrature, FP64:
+stiffness (AssemblyStiffnessFE with the P0 coefficient) and mass (AssemblyMass(1))
+CSR values plus the load vector of f = sin(pi x) sin(pi y) sin(pi z), assembled in
+one fused pass on the device-resident structural pattern, followed by closeMatrix's
+prune check of both matrices.  The mesh, DOF map and pattern are built once (timed
+separately as `setup_s`).  Inputs are synthetic (seeded), not a dataset.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 128]
+
+Prints one JSON line.  Under torchrun (N > 1) every rank assembles its own replica
+(weak scaling) and rank 0 prints the aggregate over ranks (max time over ranks).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "elements/s assembled into CSR (frac. HBM peak); batched vs plain adjoint grads/s"
+UNIT = "elements/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_inputs(n, seed=20261205):
+    from proxpde_gb300 import meshgen
+
+    xyz, conn = meshgen.cube_hex(n)
+    xyz = meshgen.perturb(xyz, n, 0.2, seed)
+    k = meshgen.lognormal(seed + 1, conn.shape[0], 1.0)
+    return xyz, conn, k
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, max clock, reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(n_sample, threads):
+    """The oracle (restated reference loop: triplets + setFromTriplets + prune) on a
+    bounded sample of the same workload; returns elements/s."""
+    import oracle as O
+
+    xyz, conn, k = make_inputs(n_sample)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    t0 = time.perf_counter()
+    O.build(O.Q1HEX, xyz, conn, em, ndof, lhs={"stiff_kind": 2, "stiff_c": 1.0, "k_e": k}, nthreads=threads)
+    O.build(O.Q1HEX, xyz, conn, em, ndof, lhs={"mass_kind": 1, "mass_c": 1.0},
+            rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0}, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return conn.shape[0] / dt, dt
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return world, rank, local
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import oracle as O
+
+    O.lib()
+    threads = os.cpu_count() or 1
+    n_sample = args.cpu_n
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, dt = cpu_sample(n_sample, threads)
+        if s >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    E = n_sample ** 3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * E / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"q1hex perturbed {args.n}^3 K+M+rhs (CPU sample {n_sample}^3)",
+                   "elements": args.n ** 3, "sample_elements": E},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n_sample}^3 Q1 hexes (of the {args.n}^3 workload), oracle OpenMP"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--cpu-n", type=int, default=40)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
+
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+
+    from proxpde_gb300 import Context, build
+    from proxpde_gb300 import _lib as L
+
+    build.build()
+    dev = local
+    torch.cuda.set_device(dev)
+    n = args.n
+    xyz, conn, k = make_inputs(n)
+    E, nn = conn.shape[0], xyz.shape[0]
+
+    t0 = time.perf_counter()
+    ctx = Context(dev)
+    ctx.set_mesh(L.Q1HEX, xyz, conn)
+    ndof = ctx.build_dofmap()
+    nnz = ctx.build_pattern()
+    ctx.set_coef(k)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    K = torch.empty(nnz, dtype=torch.float64, device=dev)
+    M = torch.empty(nnz, dtype=torch.float64, device=dev)
+    b = torch.empty(ndof, dtype=torch.float64, device=dev)
+    opK = {"stiffness": 2, "stiff_coef": 1.0}
+    opM = {"mass": 1, "mass_coef": 1.0}
+    rhs = {"kind": 1, "fn": L.FN_SIN3, "coef": 1.0}
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+
+    def step(i=None):
+        if i is not None:
+            ev[i][0].record(stream)
+        ctx.assemble(op0=opK, vals0=K, op1=opM, vals1=M, rhs=rhs, b=b, stream=sp)
+        if i is not None:
+            ev[i][1].record(stream)
+        pk = ctx.prune_count(K, stream=sp)
+        pm = ctx.prune_count(M, stream=sp)
+        return pk, pm
+
+    for _ in range(args.warmup):
+        pruned = step()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(dev)
+    clk.start()
+    time.sleep(0.3)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for i in range(args.steps):
+        pruned = step(i)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_ms = start.elapsed_time(stop)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = t.item()
+    ms_step = total_ms / args.steps
+    asm_ms = statistics.mean(a.elapsed_time(c) for a, c in ev)
+    value = world * E / (ms_step * 1e-3)
+
+    # algorithmic bytes of the fused assembly launch (conn, DOF map, k_e, xyz, two
+    # value arrays written once, load vector)
+    alg = 4 * 8 * E + 4 * 8 * E + 8 * E + 24 * nn + 8 * nnz * 2 + 8 * ndof
+    hbm, which = peaks()
+    achieved = alg / (asm_ms * 1e-3) / 1e9
+    # FP64 work of the kernel as written (flops per element)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "peak_source": which, "kernel": "kAssemble<Q1HEX> (+memset of K, M, b)",
+            "kernel_ms": asm_ms, "algorithmic_bytes": alg}
+
+    e2e = None
+    if not args.no_e2e:
+        # through the C ABI with host buffers: coordinates and coefficients uploaded
+        # from pinned memory each step, K, M, b read back into pinned memory
+        xyz_h = torch.from_numpy(xyz).pin_memory()
+        k_h = torch.from_numpy(k).pin_memory()
+        K_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+        M_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+        b_h = torch.empty(ndof, dtype=torch.float64).pin_memory()
+
+        def e2e_step():
+            ctx.set_coords(xyz_h, stream=sp)
+            ctx.set_coef(k_h, stream=sp)
+            step()
+            K_h.copy_(K, non_blocking=True)
+            M_h.copy_(M, non_blocking=True)
+            b_h.copy_(b, non_blocking=True)
+            torch.cuda.synchronize()
+
+        for _ in range(2):
+            e2e_step()
+        t1 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t1) / args.steps
+        e2e = {"value": world * E / e2e_s, "unit": UNIT, "h2d_bytes_per_step": xyz.nbytes + k.nbytes,
+               "d2h_bytes_per_step": 2 * nnz * 8 + ndof * 8, "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v_all, dt_all = cpu_sample(args.cpu_n, threads)
+        v_one, dt_one = cpu_sample(min(args.cpu_n, 24), 1)
+        cpu = {"value": v_all, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_n}^3 Q1 hexes of the same workload (K+M+rhs), oracle restatement with OpenMP",
+               "value_1thread": v_one, "sample_1thread": f"{min(args.cpu_n, 24)}^3 hexes, 1 thread"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded perturbed cube)",
+            "config": {"workload": f"q1hex perturbed {n}^3: K(k_e)+M+rhs sin3, fused pass + prune check",
+                       "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned),
+                       "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
+                       "setup_s": setup_s, "parallelism": f"replicas x{world}"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": 3 * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,189 @@
+/* pxg.h — C ABI of the GB300 finite-element assembly engine (proxpde_gb300).
+ *
+ * The engine replaces proxpde's element loop: Builder::buildLhs / buildRhs /
+ * closeMatrix (include/builder.hpp:31-154, 279-371) driving AssemblyStiffness(FE),
+ * AssemblyScalarMass and AssemblyRhsAnalytic / AssemblyS2SProjection over CurFE
+ * geometry (include/curfe.hpp:50-103) and Gauss quadrature, on P1/P2 tetrahedra and
+ * Q1/Q2 hexahedra.  Everything here is plain C: pointers, sizes and status codes.
+ *
+ * Conventions
+ *  - Every call returns a pxg_status; pxg_last_error() gives a message for the last
+ *    failing call on a context.  The reference aborts instead (assert, std::abort,
+ *    std::exit(2): include/def.hpp:273-274); here nothing aborts the process.
+ *  - `mem` arguments say where a buffer lives: PXG_MEM_HOST (the engine copies it
+ *    through its own staging) or PXG_MEM_DEVICE (a device pointer on the context's
+ *    GPU).  Assembly outputs must be device buffers unless stated otherwise.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ *    Calls are stream-ordered; host-memory variants synchronise the stream.
+ *  - One context per host thread (the reference keeps a mutable CurFE inside its
+ *    FESpace, include/fespace.hpp:190, so it is not thread-safe either).
+ *  - Index types follow the reference: DOF and vertex ids are uint32
+ *    (include/def.hpp:60-66), CSR indices are int32 like Eigen::SparseMatrix's default
+ *    StorageIndex (include/sparse_matrix.hpp:38-39).
+ */
+#ifndef PXG_H
+#define PXG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pxg_status
+{
+  PXG_OK = 0,
+  PXG_ERR_INVALID_ARG = 1,   /* bad size, null pointer, out-of-range id, wrong order of calls */
+  PXG_ERR_OOM = 2,           /* device or pinned-host allocation failed */
+  PXG_ERR_CUDA = 3,          /* a CUDA runtime call failed (message in pxg_last_error) */
+  PXG_ERR_TIMEOUT = 4,       /* a bounded device wait ran out (persistent kernels) */
+  PXG_ERR_NOT_CONVERGED = 5, /* an iterative solve stopped at its iteration limit */
+  PXG_ERR_UNSUPPORTED = 6,   /* element type / operator combination not provided */
+  PXG_ERR_NO_DEVICE = 7,     /* no CUDA device, or the requested one is absent */
+  PXG_ERR_NUMERIC = 8        /* a degenerate element (zero Jacobian) or a NaN input */
+} pxg_status;
+
+/* Element types: LagrangeFE<Tetrahedron,1|2>, LagrangeFE<Hexahedron,1|2> with their
+ * RecommendedQR (include/fe.hpp:96-131): Tet4, Tet11, Hex8 (2x2x2), Hex27 (3x3x3). */
+typedef enum pxg_elem_type
+{
+  PXG_P1TET = 0,
+  PXG_P2TET = 1,
+  PXG_Q1HEX = 2,
+  PXG_Q2HEX = 3
+} pxg_elem_type;
+
+typedef enum pxg_mem
+{
+  PXG_MEM_HOST = 0,
+  PXG_MEM_DEVICE = 1
+} pxg_mem;
+
+/* Analytic functions evaluated on the device at the quadrature points.  The
+ * reference passes a host std::function (include/assembly_rhs.hpp:50-59), which
+ * cannot run on a GPU; callers pick one of these by id instead. */
+typedef enum pxg_fn
+{
+  PXG_FN_CONST = 0,         /* f = c */
+  PXG_FN_SIN3 = 1,          /* f = c sin(pi x) sin(pi y) sin(pi z) */
+  PXG_FN_POISSON_RHS = 2,   /* f = c 2.5 pi^2 sin(pi x/2) sin(3 pi y/2)  (test/poisson3d*.cpp:27-33) */
+  PXG_FN_POISSON_EXACT = 3  /* f = c sin(pi x/2) sin(3 pi y/2)            (test/poisson3d*.cpp:35-40) */
+} pxg_fn;
+
+typedef struct pxg_ctx pxg_ctx;
+
+/* One matrix assembled by a buildLhs call (include/builder.hpp:31-154): the sum of a
+ * stiffness term and a mass term.
+ *   stiffness 0: none
+ *             1: AssemblyStiffness(stiff_coef)          (include/assembly_lhs.hpp:36-75)
+ *             2: AssemblyStiffnessFE with the per-element (P0 FEVar) coefficient set by
+ *                pxg_set_coef, times stiff_coef         (include/assembly_lhs.hpp:77-113)
+ *   mass      0: none, 1: AssemblyScalarMass(mass_coef) (include/assembly_lhs.hpp:191-231)
+ *   apply_bc  condense with the context's essential BCs (include/builder.hpp:76-124);
+ *             the lifted load C(-Ke h) and h at constrained DOFs go into b as the
+ *             reference's buildLhs does (builder.hpp:102, 119, 137). */
+typedef struct pxg_lhs_op
+{
+  int32_t stiffness;
+  double stiff_coef;
+  int32_t mass;
+  double mass_coef;
+  int32_t apply_bc;
+} pxg_lhs_op;
+
+/* One load vector term of a buildRhs call (include/builder.hpp:279-364).
+ *   kind 0: none
+ *        1: AssemblyRhsAnalytic with function `fn` scaled by `coef`
+ *           (include/assembly_rhs.hpp:34-91), f evaluated at CurFE::qpoint
+ *        2: AssemblyS2SProjection(coef, field) of a DOF vector on the same space
+ *           (include/assembly_rhs.hpp:93-163); `field` is a device pointer (ndof)
+ *   apply_bc  zero constrained rows (C*Fe, builder.hpp:319-347). */
+typedef struct pxg_rhs_op
+{
+  int32_t kind;
+  int32_t fn;
+  double coef;
+  const double * field;
+  int32_t apply_bc;
+} pxg_rhs_op;
+
+/* pxg_assemble flags */
+#define PXG_ACCUMULATE 1u /* add into vals0/vals1/b instead of overwriting them */
+
+/* ----------------------------------------------------------------- context */
+pxg_status pxg_create(pxg_ctx ** ctx, int device);
+pxg_status pxg_destroy(pxg_ctx * ctx);
+const char * pxg_last_error(const pxg_ctx * ctx);
+const char * pxg_status_string(pxg_status s);
+/* Version of this ABI (major * 10000 + minor * 100 + patch). */
+int pxg_version(void);
+
+/* ------------------------------------------------------------ mesh input
+ * Mesh<Elem>{pointList, elementList} (include/mesh.hpp:74-100): node coordinates
+ * xyz[nnodes][3] and vertex connectivity conn[nelem][nv] (nv = 4 tets, 8 hexes) in
+ * the reference's local vertex order (include/geo.hpp:508-760).  Element ids are the
+ * row indices.  Replaces any previous mesh (and drops the DOF map and pattern). */
+pxg_status pxg_set_mesh(pxg_ctx * ctx, int elem_type, const double * xyz, int64_t nnodes,
+                        const uint32_t * conn, int64_t nelem, int mem);
+/* Overwrite the node coordinates of the current mesh (same connectivity). */
+pxg_status pxg_set_coords(pxg_ctx * ctx, const double * xyz, int mem, void * stream);
+
+/* --------------------------------------------------------------- DOF map
+ * DOF::setupElemMap first-touch numbering (include/dof.hpp:111-329), computed on the
+ * device: a DOF gets the next id the first time the element loop meets its entity
+ * (points, then edges, then faces, then the element).  elemMap is nelem x ndofs/elem,
+ * row-major, like DOF::elemMap (a Table, include/def.hpp:111-127). */
+pxg_status pxg_build_dofmap(pxg_ctx * ctx, int64_t * ndof);
+/* Use a caller-provided DOF map instead (e.g. proxpde's own dof.elemMap). */
+pxg_status pxg_set_dofmap(pxg_ctx * ctx, const uint32_t * elem_map, int64_t ndof, int mem);
+pxg_status pxg_get_dofmap(pxg_ctx * ctx, uint32_t * elem_map, int mem);
+
+/* --------------------------------------------------------- CSR pattern
+ * The structural pattern of every (idI, idJ) pair the element loop emits
+ * (builder.hpp:131-152), sorted by row then column: the pattern Eigen's
+ * setFromTriplets builds (builder.hpp:368) before prune.  Built on the device once
+ * per mesh; it also builds the per-element scatter map used by pxg_assemble. */
+pxg_status pxg_build_pattern(pxg_ctx * ctx, int64_t * nnz);
+pxg_status pxg_get_pattern(pxg_ctx * ctx, int32_t * row_ptr, int32_t * col_idx, int mem);
+/* Device pointers of the context-owned structural pattern (valid until the mesh
+ * changes). */
+pxg_status pxg_pattern_device(pxg_ctx * ctx, const int32_t ** row_ptr, const int32_t ** col_idx);
+
+/* ----------------------------------------------------- coefficients, BCs
+ * Per-element coefficient k_e (a P0 FEVar, include/var.hpp:56-127), nelem values. */
+pxg_status pxg_set_coef(pxg_ctx * ctx, const double * k_e, int mem, void * stream);
+/* Essential BCs: BCEss (include/bc.hpp:32-306) merged into one constrained-DOF list
+ * with values; `diag` is BCEss::diag (1.0 in the reference, bc.hpp:301).  n = 0
+ * clears the BCs.  A DOF listed twice keeps the last value, as the reference's
+ * builder keeps the value of the last BC that constrains it (builder.hpp:85-100). */
+pxg_status pxg_set_bc(pxg_ctx * ctx, const uint32_t * dofs, const double * vals, int64_t n,
+                      double diag, int mem);
+
+/* --------------------------------------------------------------- assembly
+ * One fused pass over the elements: up to two matrices (vals0/vals1, each nnz long on
+ * the structural pattern, device memory) and one load vector b (ndof, device).
+ * Any of op0/op1/rhs may be NULL (and then its output is untouched).  b receives the
+ * rhs term plus the BC lifts of the lhs ops that apply BCs. */
+pxg_status pxg_assemble(pxg_ctx * ctx, const pxg_lhs_op * op0, double * vals0,
+                        const pxg_lhs_op * op1, double * vals1, const pxg_rhs_op * rhs,
+                        double * b, unsigned flags, void * stream);
+
+/* Builder::closeMatrix's prune(1., 1e-16) (builder.hpp:369): count the entries of a
+ * structural-pattern value array with |v| <= 1e-16.  0 means the structural pattern
+ * and `vals` already are the closed matrix. */
+pxg_status pxg_prune_count(pxg_ctx * ctx, const double * vals, int64_t * pruned, void * stream);
+/* Compact: write the pruned CSR (row_ptr[ndof+1], col_idx, vals_out; device
+ * pointers, capacity nnz) and its entry count. */
+pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_ptr,
+                            int32_t * col_idx, double * vals_out, int64_t * nnz_out,
+                            void * stream);
+
+/* Lagrange interpolation of an analytic function at the DOF points
+ * (interpolateAnalyticFunction, include/fespace.hpp:195-271): v[ndof], device. */
+pxg_status pxg_interpolate(pxg_ctx * ctx, int fn, double coef, double * v, void * stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PXG_H */

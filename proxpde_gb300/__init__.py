@@ -1,0 +1,336 @@
+"""proxpde_gb300 — GB300 finite-element assembly engine with proxpde's Builder interface.
+
+The names below mirror proxpde's C++ API for the assembly path so that code (and the
+parity tests) read like proxpde's own tests (e.g. test/poisson3dhex.cpp:46-74):
+
+    mesh = buildHyperCube(Hexahedron, n)                    # include/mesh.hpp:385-421
+    fe = FESpace(mesh, order=1)                             # include/fespace.hpp:27-193
+    bcs = [BCEss(fe, side.LEFT), BCEss(fe, side.BOTTOM)]    # include/bc.hpp:32-306
+    builder = Builder(fe)                                   # include/builder.hpp:12-391
+    builder.buildLhs((AssemblyStiffness(1.0, fe),), bcs)
+    builder.buildRhs((AssemblyRhsAnalytic(FN_POISSON_RHS, fe),), bcs)
+    builder.closeMatrix()
+    builder.A  (scipy CSR on the host) / builder.A_dev (device CSR)  builder.b
+
+Every computation runs on the GPU through libpxg.so (include/pxg.h); there is no CPU
+path.  A host std::function rhs has no device equivalent, so analytic right-hand
+sides are chosen by id (FN_*).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import meshgen
+from ._lib import (FN_CONST, FN_POISSON_EXACT, FN_POISSON_RHS, FN_SIN3, P1TET, P2TET, Q1HEX, Q2HEX, Context,
+                   PxgError, load)
+
+__all__ = [
+    "Tetrahedron", "Hexahedron", "Mesh", "buildHyperCube", "FESpace", "BCEss", "side", "Builder",
+    "AssemblyStiffness", "AssemblyStiffnessFE", "AssemblyScalarMass", "AssemblyMass", "AssemblyRhsAnalytic",
+    "AssemblyS2SProjection", "AssemblyProjection", "interpolateAnalyticFunction", "Context", "PxgError",
+    "FN_CONST", "FN_SIN3", "FN_POISSON_RHS", "FN_POISSON_EXACT", "P1TET", "P2TET", "Q1HEX", "Q2HEX", "meshgen",
+    "load",
+]
+
+
+class Tetrahedron:
+    nv = 4
+
+
+class Hexahedron:
+    nv = 8
+
+
+class side:
+    """Boundary markers of the structured cube (include/mesh.hpp:178-188)."""
+    NONE, BOTTOM, RIGHT, TOP, LEFT, BACK, FRONT = 0, 1, 2, 3, 4, 5, 6
+    # plane of each marker as set by markFacetsCube (include/mesh.hpp:442-498)
+    PLANE = {1: (1, 0.0), 2: (0, 1.0), 3: (1, 1.0), 4: (0, 0.0), 5: (2, 0.0), 6: (2, 1.0)}
+
+
+class Mesh:
+    """Mesh<Elem>{pointList, elementList} as arrays: xyz[nnodes,3], conn[nelem,nv]."""
+
+    def __init__(self, elem, xyz, conn, facets=None):
+        self.elem = elem
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.uint32)
+        # optional tagged boundary facets: (vertex ids array [nf, k], markers [nf])
+        self.facets = facets
+
+
+def buildHyperCube(elem, n: int) -> Mesh:
+    """buildCube on [0,1]^3 with n^3 cubes (src/mesh.cpp:355-534): hexahedra, or 5
+    tetrahedra per cube."""
+    if elem is Hexahedron:
+        xyz, conn = meshgen.cube_hex(n)
+    else:
+        xyz, conn = meshgen.cube_tet5(n)
+    m = Mesh(elem, xyz, conn)
+    m.structured_n = n
+    return m
+
+
+def _etype(elem, order):
+    if elem is Tetrahedron:
+        return {1: P1TET, 2: P2TET}[order]
+    return {1: Q1HEX, 2: Q2HEX}[order]
+
+
+class _Dof:
+    def __init__(self, fe):
+        self._fe = fe
+        self.size = fe.ctx.ndof
+        self._em = None
+
+    @property
+    def elemMap(self):
+        if self._em is None:
+            self._em = self._fe.ctx.get_dofmap()
+        return self._em
+
+    def getId(self, e, i):
+        return int(self.elemMap[e, i])
+
+
+class FESpace:
+    """FESpace<Mesh, LagrangeFE<Elem, order>::RefFE_T, RecommendedQR>: owns the device
+    context with the mesh, the first-touch DOF map and the CSR pattern."""
+
+    def __init__(self, mesh: Mesh, order: int = 1, device: int = 0, elem_map=None, ndof=None):
+        self.mesh = mesh
+        self.order = order
+        self.etype = _etype(mesh.elem, order)
+        self.ctx = Context(device)
+        self.ctx.set_mesh(self.etype, mesh.xyz, mesh.conn)
+        if elem_map is None:
+            self.ctx.build_dofmap()
+        else:
+            self.ctx.set_dofmap(np.ascontiguousarray(elem_map, dtype=np.uint32), ndof)
+        self.dof = _Dof(self)
+        self._pattern = False
+        self._bc_key = None
+
+    def pattern(self):
+        if not self._pattern:
+            self.ctx.build_pattern()
+            self._pattern = True
+        return self.ctx.nnz
+
+    def dofPts(self):
+        """Coordinates of every DOF (RefFE::dofPts scattered by the DOF map)."""
+        return np.stack([_interp_coord(self, d) for d in range(3)], axis=1)
+
+    def set_coefficient(self, k_e):
+        self.ctx.set_coef(np.ascontiguousarray(k_e, dtype=np.float64))
+
+    def apply_bcs(self, bcs):
+        key = tuple(id(b) for b in bcs)
+        if key == self._bc_key:
+            return
+        if not bcs:
+            self.ctx.set_bc(np.zeros(0, np.uint32), np.zeros(0), 1.0)
+        else:
+            dofs = np.concatenate([b.dofs for b in bcs]).astype(np.uint32)
+            vals = np.concatenate([b.values for b in bcs])
+            self.ctx.set_bc(dofs, vals, bcs[-1].diag)
+        self._bc_key = key
+
+
+def _interp_coord(fe, d):
+    # DOF coordinates from the mesh: vertices directly, higher-order DOFs as the
+    # averages RefFE::dofPts forms (include/reffe.hpp:748-767, 960-988)
+    em = fe.dof.elemMap
+    X = fe.mesh.xyz[fe.mesh.conn.astype(np.int64)][:, :, d]
+    cols = [X[:, a] for a in range(X.shape[1])]
+    if fe.etype == P2TET:
+        for a, b in ((0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)):
+            cols.append(.5 * (X[:, a] + X[:, b]))
+    if fe.etype == Q2HEX:
+        for a, b in ((0, 1), (1, 2), (2, 3), (3, 0), (0, 4), (1, 5), (2, 6), (3, 7), (4, 5), (5, 6), (6, 7), (7, 4)):
+            cols.append(0.5 * (X[:, a] + X[:, b]))
+        for f in ((0, 3, 2, 1), (3, 0, 4, 7), (0, 1, 5, 4), (1, 2, 6, 5), (2, 3, 7, 6), (4, 5, 6, 7)):
+            cols.append(0.25 * (X[:, f[0]] + X[:, f[1]] + X[:, f[2]] + X[:, f[3]]))
+        s = X[:, 0]
+        for a in range(1, 8):
+            s = s + X[:, a]
+        cols.append(.125 * s)
+    P = np.stack(cols, axis=1)
+    out = np.zeros(fe.dof.size)
+    out[em.reshape(-1).astype(np.int64)] = P.reshape(-1)
+    return out
+
+
+class BCEss:
+    """Essential BC on the DOFs of the boundary facets with a marker (bc.hpp:252-295),
+    or on an explicit DOF list.  ``value`` is a constant or an array per DOF."""
+
+    def __init__(self, fe: FESpace, marker=None, value=0.0, dofs=None, diag=1.0):
+        self.fe = fe
+        self.diag = float(diag)
+        if dofs is None:
+            dofs = self._marker_dofs(fe, marker)
+        self.dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
+        v = np.asarray(value, dtype=np.float64)
+        self.values = np.broadcast_to(v, self.dofs.shape).copy() if v.ndim == 0 else v.copy()
+
+    @staticmethod
+    def _marker_dofs(fe, marker):
+        m = fe.mesh
+        if m.facets is not None:
+            # tagged facets: a Lagrange facet carries the DOFs of its vertices (P1/Q1)
+            verts, tags = m.facets
+            sel = np.unique(verts[tags == marker].reshape(-1))
+            if fe.etype not in (P1TET, Q1HEX):
+                raise NotImplementedError("tagged-facet BCs are provided for P1/Q1 spaces")
+            em, conn = fe.dof.elemMap, m.conn
+            nv = conn.shape[1]
+            node2dof = np.full(m.xyz.shape[0], -1, dtype=np.int64)
+            node2dof[conn.reshape(-1).astype(np.int64)] = em[:, :nv].reshape(-1)
+            return node2dof[sel]
+        # structured cube: the facets markFacetsCube tags with `marker` lie on one plane
+        axis, val = side.PLANE[marker]
+        x = _interp_coord(fe, axis)
+        return np.nonzero(np.abs(x - val) <= 1e-6)[0]
+
+
+# ----------------------------------------------------------------- assemblies
+class AssemblyStiffness:
+    """AssemblyStiffness(c, feSpace) (include/assembly_lhs.hpp:36-75)."""
+
+    def __init__(self, coef, fe):
+        self.fe, self.op = fe, {"stiffness": 1, "stiff_coef": float(coef)}
+
+
+class AssemblyStiffnessFE:
+    """AssemblyStiffnessFE(coefP0, feSpace) with a per-element (P0) coefficient
+    (include/assembly_lhs.hpp:77-113)."""
+
+    def __init__(self, k_e, fe, scale=1.0):
+        fe.set_coefficient(k_e)
+        self.fe, self.op = fe, {"stiffness": 2, "stiff_coef": float(scale)}
+
+
+class AssemblyScalarMass:
+    """AssemblyScalarMass / AssemblyMass(c, feSpace) (include/assembly_lhs.hpp:191-231, 347-365)."""
+
+    def __init__(self, coef, fe):
+        self.fe, self.op = fe, {"mass": 1, "mass_coef": float(coef)}
+
+
+AssemblyMass = AssemblyScalarMass
+
+
+class AssemblyRhsAnalytic:
+    """AssemblyRhsAnalytic(f, feSpace) with f chosen by id (include/assembly_rhs.hpp:34-91)."""
+
+    def __init__(self, fn, fe, coef=1.0):
+        self.fe, self.rhs = fe, {"kind": 1, "fn": int(fn), "coef": float(coef)}
+
+
+class AssemblyS2SProjection:
+    """AssemblyS2SProjection(c, field, feSpace) (include/assembly_rhs.hpp:93-163)."""
+
+    def __init__(self, coef, field, fe):
+        import torch
+
+        self.field = torch.as_tensor(np.ascontiguousarray(field, dtype=np.float64)).to(f"cuda:{fe.ctx.device}")
+        self.fe, self.rhs = fe, {"kind": 2, "coef": float(coef), "field": self.field}
+
+
+AssemblyProjection = AssemblyS2SProjection
+
+
+def interpolateAnalyticFunction(fn, fe, coef=1.0):
+    """interpolateAnalyticFunction (include/fespace.hpp:195-271) on the device."""
+    import torch
+
+    v = torch.zeros(fe.dof.size, dtype=torch.float64, device=f"cuda:{fe.ctx.device}")
+    fe.ctx.interpolate(fn, coef, v)
+    torch.cuda.synchronize()
+    return v.cpu().numpy()
+
+
+class Builder:
+    """Builder (include/builder.hpp:12-391): buildLhs / buildRhs accumulate into a
+    device value array on the structural pattern and into b; closeMatrix prunes
+    |v| <= 1e-16 and exposes the CSR (A on the host as scipy, A_dev on the device)."""
+
+    def __init__(self, fe: FESpace):
+        import torch
+
+        self.fe = fe
+        self.dev = f"cuda:{fe.ctx.device}"
+        fe.pattern()
+        self.vals = torch.zeros(fe.ctx.nnz, dtype=torch.float64, device=self.dev)
+        self.b_dev = torch.zeros(fe.dof.size, dtype=torch.float64, device=self.dev)
+        self.A = None
+        self.A_dev = None
+
+    def buildLhs(self, assemblies, bcs=()):
+        op = {"stiffness": 0, "stiff_coef": 0.0, "mass": 0, "mass_coef": 0.0, "apply_bc": 1 if bcs else 0}
+        if len(assemblies) == 0:
+            raise ValueError("we need at least 1 assembly.")
+        for a in assemblies:
+            o = getattr(a, "op", None)
+            if o is None:
+                raise PxgError(6, f"{type(a).__name__} is not a matrix assembly known to the engine")
+            if "stiffness" in o:
+                if op["stiffness"]:
+                    raise PxgError(6, "one stiffness term per buildLhs call")
+                op["stiffness"], op["stiff_coef"] = o["stiffness"], o["stiff_coef"]
+            if "mass" in o:
+                if op["mass"]:
+                    raise PxgError(6, "one mass term per buildLhs call")
+                op["mass"], op["mass_coef"] = o["mass"], o["mass_coef"]
+        self.fe.apply_bcs(list(bcs))
+        self.fe.ctx.assemble(op0=op, vals0=self.vals, b=self.b_dev if bcs else None, accumulate=True)
+
+    def buildRhs(self, assemblies, bcs=()):
+        self.fe.apply_bcs(list(bcs))
+        for a in assemblies:
+            r = dict(a.rhs)
+            r["apply_bc"] = 1 if bcs else 0
+            self.fe.ctx.assemble(rhs=r, b=self.b_dev, accumulate=True)
+
+    def closeMatrix(self):
+        import scipy.sparse as sp
+        import torch
+
+        ctx = self.fe.ctx
+        rp_s, ci_s = ctx.pattern_device()
+        n = self.fe.dof.size
+        if ctx.prune_count(self.vals) == 0:
+            rp = torch.empty(n + 1, dtype=torch.int32, device=self.dev)
+            ci = torch.empty(ctx.nnz, dtype=torch.int32, device=self.dev)
+            rph, cih = ctx.get_pattern()
+            rp.copy_(torch.from_numpy(rph))
+            ci.copy_(torch.from_numpy(cih))
+            vals = self.vals.clone()
+        else:
+            rp = torch.empty(n + 1, dtype=torch.int32, device=self.dev)
+            ci = torch.empty(ctx.nnz, dtype=torch.int32, device=self.dev)
+            vals = torch.empty(ctx.nnz, dtype=torch.float64, device=self.dev)
+            nnz = ctx.close_matrix(self.vals, rp, ci, vals)
+            ci, vals = ci[:nnz], vals[:nnz]
+        torch.cuda.synchronize()
+        self.A_dev = (rp, ci, vals)
+        self.A = sp.csr_matrix((vals.cpu().numpy(), ci.cpu().numpy(), rp.cpu().numpy()), shape=(n, n))
+        self.vals.zero_()  # setFromTriplets consumed the triplets (builder.hpp:370)
+
+    @property
+    def b(self):
+        import torch
+
+        torch.cuda.synchronize()
+        return self.b_dev.cpu().numpy()
+
+    def clearRhs(self):
+        self.b_dev.zero_()
+
+    def clearLhs(self):
+        self.vals.zero_()
+
+    def clear(self):
+        self.clearLhs()
+        self.clearRhs()

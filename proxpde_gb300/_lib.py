@@ -1,0 +1,236 @@
+"""ctypes binding of the engine's C ABI (include/pxg.h, library proxpde_gb300/libpxg.so).
+
+There is no fallback: if the library is missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpxg.so")
+
+P1TET, P2TET, Q1HEX, Q2HEX = 0, 1, 2, 3
+MEM_HOST, MEM_DEVICE = 0, 1
+FN_CONST, FN_SIN3, FN_POISSON_RHS, FN_POISSON_EXACT = 0, 1, 2, 3
+ACCUMULATE = 1
+
+STATUS = {
+    0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "timeout",
+    5: "not converged", 6: "unsupported", 7: "no CUDA device", 8: "numerical error",
+}
+
+# every symbol include/pxg.h declares (checked by the CPU tests)
+EXPORTS = [
+    "pxg_create", "pxg_destroy", "pxg_last_error", "pxg_status_string", "pxg_version",
+    "pxg_set_mesh", "pxg_set_coords", "pxg_build_dofmap", "pxg_set_dofmap", "pxg_get_dofmap",
+    "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
+    "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate",
+]
+
+
+class PxgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class LhsOp(C.Structure):
+    _fields_ = [
+        ("stiffness", C.c_int32),
+        ("stiff_coef", C.c_double),
+        ("mass", C.c_int32),
+        ("mass_coef", C.c_double),
+        ("apply_bc", C.c_int32),
+    ]
+
+
+class RhsOp(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("fn", C.c_int32),
+        ("coef", C.c_double),
+        ("field", C.c_void_p),
+        ("apply_bc", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libpxg.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build the engine first (python -m proxpde_gb300.build)")
+    L = C.CDLL(path)
+    vp, i64, i64p = C.c_void_p, C.c_int64, C.POINTER(C.c_int64)
+    sig = {
+        "pxg_create": ([C.POINTER(vp), C.c_int], C.c_int),
+        "pxg_destroy": ([vp], C.c_int),
+        "pxg_last_error": ([vp], C.c_char_p),
+        "pxg_status_string": ([C.c_int], C.c_char_p),
+        "pxg_version": ([], C.c_int),
+        "pxg_set_mesh": ([vp, C.c_int, vp, i64, vp, i64, C.c_int], C.c_int),
+        "pxg_set_coords": ([vp, vp, C.c_int, vp], C.c_int),
+        "pxg_build_dofmap": ([vp, i64p], C.c_int),
+        "pxg_set_dofmap": ([vp, vp, i64, C.c_int], C.c_int),
+        "pxg_get_dofmap": ([vp, vp, C.c_int], C.c_int),
+        "pxg_build_pattern": ([vp, i64p], C.c_int),
+        "pxg_get_pattern": ([vp, vp, vp, C.c_int], C.c_int),
+        "pxg_pattern_device": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int),
+        "pxg_set_coef": ([vp, vp, C.c_int, vp], C.c_int),
+        "pxg_set_bc": ([vp, vp, vp, i64, C.c_double, C.c_int], C.c_int),
+        "pxg_assemble": ([vp, C.POINTER(LhsOp), vp, C.POINTER(LhsOp), vp, C.POINTER(RhsOp), vp, C.c_uint, vp],
+                         C.c_int),
+        "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
+        "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
+        "pxg_interpolate": ([vp, C.c_int, C.c_double, vp, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    """Address of a numpy array (host) or a torch tensor (device or host)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return a.ctypes.data
+    if isinstance(a, int):
+        return a
+    assert a.is_contiguous()
+    return a.data_ptr()
+
+
+def _mem(a):
+    if isinstance(a, np.ndarray):
+        return MEM_HOST
+    if isinstance(a, int):
+        return MEM_DEVICE
+    return MEM_DEVICE if a.is_cuda else MEM_HOST
+
+
+class Context:
+    """One engine context (pxg_ctx) bound to a GPU."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        st = self.L.pxg_create(C.byref(h), device)
+        if st != 0:
+            raise PxgError(st, "pxg_create")
+        self.h = h
+        self.device = device
+        self.ndof = 0
+        self.nnz = 0
+        self.nelem = 0
+        self.etype = None
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.L.pxg_last_error(self.h)
+            raise PxgError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pxg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- inputs
+    def set_mesh(self, etype, xyz, conn):
+        self.etype = etype
+        self.nelem = int(conn.shape[0])
+        self._check(self.L.pxg_set_mesh(self.h, etype, _ptr(xyz), int(xyz.shape[0]), _ptr(conn), self.nelem,
+                                        _mem(xyz)), "set_mesh")
+
+    def set_coords(self, xyz, stream=None):
+        self._check(self.L.pxg_set_coords(self.h, _ptr(xyz), _mem(xyz), stream), "set_coords")
+
+    def build_dofmap(self):
+        n = C.c_int64()
+        self._check(self.L.pxg_build_dofmap(self.h, C.byref(n)), "build_dofmap")
+        self.ndof = n.value
+        return self.ndof
+
+    def set_dofmap(self, em, ndof):
+        self._check(self.L.pxg_set_dofmap(self.h, _ptr(em), int(ndof), _mem(em)), "set_dofmap")
+        self.ndof = int(ndof)
+
+    def get_dofmap(self):
+        N = {P1TET: 4, P2TET: 10, Q1HEX: 8, Q2HEX: 27}[self.etype]
+        em = np.zeros((self.nelem, N), dtype=np.uint32)
+        self._check(self.L.pxg_get_dofmap(self.h, _ptr(em), MEM_HOST), "get_dofmap")
+        return em
+
+    def build_pattern(self):
+        n = C.c_int64()
+        self._check(self.L.pxg_build_pattern(self.h, C.byref(n)), "build_pattern")
+        self.nnz = n.value
+        return self.nnz
+
+    def get_pattern(self):
+        rp = np.zeros(self.ndof + 1, dtype=np.int32)
+        ci = np.zeros(self.nnz, dtype=np.int32)
+        self._check(self.L.pxg_get_pattern(self.h, _ptr(rp), _ptr(ci), MEM_HOST), "get_pattern")
+        return rp, ci
+
+    def pattern_device(self):
+        rp, ci = C.c_void_p(), C.c_void_p()
+        self._check(self.L.pxg_pattern_device(self.h, C.byref(rp), C.byref(ci)), "pattern_device")
+        return rp.value, ci.value
+
+    def set_coef(self, k_e, stream=None):
+        self._check(self.L.pxg_set_coef(self.h, _ptr(k_e), _mem(k_e), stream), "set_coef")
+
+    def set_bc(self, dofs, vals, diag=1.0):
+        dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self._check(self.L.pxg_set_bc(self.h, _ptr(dofs), _ptr(vals), int(dofs.size), float(diag), MEM_HOST),
+                    "set_bc")
+
+    # --- assembly
+    def assemble(self, op0=None, vals0=None, op1=None, vals1=None, rhs=None, b=None, accumulate=False,
+                 stream=None):
+        def lhs(o):
+            if o is None:
+                return None
+            return C.pointer(LhsOp(int(o.get("stiffness", 0)), float(o.get("stiff_coef", 1.0)),
+                                   int(o.get("mass", 0)), float(o.get("mass_coef", 1.0)),
+                                   int(o.get("apply_bc", 0))))
+
+        r = None
+        if rhs is not None:
+            r = C.pointer(RhsOp(int(rhs.get("kind", 0)), int(rhs.get("fn", 0)), float(rhs.get("coef", 1.0)),
+                                _ptr(rhs.get("field")), int(rhs.get("apply_bc", 0))))
+        self._check(self.L.pxg_assemble(self.h, lhs(op0), _ptr(vals0), lhs(op1), _ptr(vals1), r, _ptr(b),
+                                        ACCUMULATE if accumulate else 0, stream), "assemble")
+
+    def prune_count(self, vals, stream=None):
+        n = C.c_int64()
+        self._check(self.L.pxg_prune_count(self.h, _ptr(vals), C.byref(n), stream), "prune_count")
+        return n.value
+
+    def close_matrix(self, vals, rp, ci, vout, stream=None):
+        n = C.c_int64()
+        self._check(self.L.pxg_close_matrix(self.h, _ptr(vals), _ptr(rp), _ptr(ci), _ptr(vout), C.byref(n), stream),
+                    "close_matrix")
+        return n.value
+
+    def interpolate(self, fn, coef, v, stream=None):
+        self._check(self.L.pxg_interpolate(self.h, int(fn), float(coef), _ptr(v), stream), "interpolate")

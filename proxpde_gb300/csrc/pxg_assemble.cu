@@ -1,0 +1,861 @@
+// Element kernels of the GB300 assembly engine.
+//
+// One thread per element computes, in FP64, what proxpde's element loop computes per
+// element (include/builder.hpp:53-153): CurFE geometry (include/curfe.hpp:50-103),
+// the stiffness / mass matrices (include/assembly_lhs.hpp:52-65, 93-109, 207-221) and
+// the load vector (include/assembly_rhs.hpp:61-88, 130-159), applies the Dirichlet
+// condensation (builder.hpp:76-124), and adds the result into CSR values and the
+// load vector with FP64 reductions (red.global.add.f64) at positions given by the
+// per-element scatter map.  The same arithmetic, rearranged:
+//   - J^+ = (J^T J)^-1 J^T and sqrt(det(J^T J)) are, for square J, J^-1 and |det J|;
+//     they are formed from the adjugate: J^-1 J^-T = adj adj^T / det^2.
+//   - Stiffness entries use the symmetric geometric factor G_q = w_q adj adj^T/|det|:
+//     K_ij = sum_q dphiRef_i(q)^T G_q dphiRef_j(q); only j >= i is computed and both
+//     (i,j) and (j,i) are written.
+//   - On tetrahedra (affine map) G is constant and K_ij = sum_ab G_ab T_ab(ij) with
+//     the reference tensors T_ab(ij) = sum_q w_q dphiRef_ia(q) dphiRef_jb(q), which
+//     are computed once from the same quadrature rule.
+// Round-off differs from the reference's Eigen evaluation order; values agree to
+// ~1e-15 relative.
+#include <cub/cub.cuh>
+
+#include <cmath>
+#include <vector>
+
+#include "pxg_internal.h"
+
+namespace pxg
+{
+
+// ------------------------------------------------------------ constant tables
+__constant__ double cP1phi[4 * 4], cP1dphi[4 * 3], cP1w[4], cP1xi[4 * 3], cP1T[6 * 16], cP1M[16];
+__constant__ double cP2phi[11 * 10], cP2dphi[11 * 10 * 3], cP2w[11], cP2xi[11 * 3], cP2T[6 * 100],
+    cP2M[100];
+__constant__ double cQ1phi[8 * 8], cQ1dphi[8 * 8 * 3], cQ1w[8], cQ1xi[8 * 3];
+__constant__ double cQ2phi[27 * 27], cQ2dphi[27 * 27 * 3], cQ2w[27], cQ2xi[27 * 3];
+
+template <int T>
+__device__ __forceinline__ double PHI(int q, int i)
+{
+  if constexpr (T == P1TET)
+    return cP1phi[q * 4 + i];
+  else if constexpr (T == P2TET)
+    return cP2phi[q * 10 + i];
+  else if constexpr (T == Q1HEX)
+    return cQ1phi[q * 8 + i];
+  else
+    return cQ2phi[q * 27 + i];
+}
+template <int T>
+__device__ __forceinline__ double DPHI(int q, int i, int d)
+{
+  if constexpr (T == P1TET)
+    return cP1dphi[i * 3 + d];
+  else if constexpr (T == P2TET)
+    return cP2dphi[(q * 10 + i) * 3 + d];
+  else if constexpr (T == Q1HEX)
+    return cQ1dphi[(q * 8 + i) * 3 + d];
+  else
+    return cQ2dphi[(q * 27 + i) * 3 + d];
+}
+template <int T>
+__device__ __forceinline__ double WQ(int q)
+{
+  if constexpr (T == P1TET)
+    return cP1w[q];
+  else if constexpr (T == P2TET)
+    return cP2w[q];
+  else if constexpr (T == Q1HEX)
+    return cQ1w[q];
+  else
+    return cQ2w[q];
+}
+template <int T>
+__device__ __forceinline__ double XI(int q, int d)
+{
+  if constexpr (T == P1TET)
+    return cP1xi[q * 3 + d];
+  else if constexpr (T == P2TET)
+    return cP2xi[q * 3 + d];
+  else if constexpr (T == Q1HEX)
+    return cQ1xi[q * 3 + d];
+  else
+    return cQ2xi[q * 3 + d];
+}
+template <int T>
+__device__ __forceinline__ double TT(int c, int i, int j)
+{
+  if constexpr (T == P1TET)
+    return cP1T[(c * 4 + i) * 4 + j];
+  else
+    return cP2T[(c * 10 + i) * 10 + j];
+}
+template <int T>
+__device__ __forceinline__ double MHAT(int i, int j)
+{
+  if constexpr (T == P1TET)
+    return cP1M[i * 4 + j];
+  else
+    return cP2M[i * 10 + j];
+}
+
+// ------------------------------------------------- host reference elements
+// Quadrature rules and shape functions of proxpde (src/qr.cpp:27, 38, 199-320;
+// src/reffe.cpp:246-253, 374-383, 510-1003), restated for the engine's tables.
+namespace
+{
+constexpr double kSqrt13rd = 0.5773502691896258; // src/qr.cpp:27
+constexpr double kSqrt35th = 0.774596669241483;  // src/qr.cpp:38
+
+void ruleHost(int t, std::vector<double> & xi, std::vector<double> & w)
+{
+  xi.clear();
+  w.clear();
+  if (t == P1TET)
+  {
+    double const a = 0.1381966011250105, b = 0.5854101966249685;
+    xi = {a, a, a, b, a, a, a, b, a, a, a, b};
+    w.assign(4, .25 / 6);
+  }
+  else if (t == P2TET)
+  {
+    double const c1 = 0.0714285714285714, c2 = 0.7857142857142857;
+    double const d1 = 0.399403576166799, d2 = 0.100596423833201;
+    xi = {0.25, 0.25, 0.25, c1, c1, c1, c2, c1, c1, c1, c2, c1, c1, c1, c2, d1, d1,
+          d2,   d1,   d2,   d1, d2, d1, d1, d1, d2, d2, d2, d1, d2, d2, d2, d1};
+    double const w0 = -0.0131555555555556, w1 = 0.0076222222222222, w2 = 0.024888888888889;
+    w = {w0, w1, w1, w1, w1, w2, w2, w2, w2, w2, w2};
+  }
+  else if (t == Q1HEX)
+  {
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i)
+        {
+          xi.push_back(i ? kSqrt13rd : -kSqrt13rd);
+          xi.push_back(j ? kSqrt13rd : -kSqrt13rd);
+          xi.push_back(k ? kSqrt13rd : -kSqrt13rd);
+          w.push_back(1.0);
+        }
+  }
+  else
+  {
+    double const x[3] = {-kSqrt35th, 0.0, kSqrt35th};
+    double const w1[3] = {5., 8., 5.};
+    for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+        {
+          xi.push_back(x[i]);
+          xi.push_back(x[j]);
+          xi.push_back(x[k]);
+          w.push_back((w1[i] * w1[j] * w1[k]) / 729.);
+        }
+  }
+}
+
+double f1(int a, double x) { return a == 0 ? 0.5 * (1. - x) : 0.5 * (1. + x); }
+double g1(int a, double) { return a == 0 ? -0.5 : 0.5; }
+double f2(int a, double x) { return a == 0 ? 0.5 * x * (x - 1.) : (a == 1 ? 0.5 * x * (x + 1.) : 1. - x * x); }
+double g2(int a, double x) { return a == 0 ? x - 0.5 : (a == 1 ? x + 0.5 : -2. * x); }
+
+// 1D factor index per axis for Q1/Q2 nodes (src/reffe.cpp:684-1003 ordering)
+constexpr int kQ1idx[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                              {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+constexpr int kQ2idx[27][3] = {
+    {0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1},
+    {0, 1, 1}, {2, 0, 0}, {1, 2, 0}, {2, 1, 0}, {0, 2, 0}, {0, 0, 2}, {1, 0, 2},
+    {1, 1, 2}, {0, 1, 2}, {2, 0, 1}, {1, 2, 1}, {2, 1, 1}, {0, 2, 1}, {2, 2, 0},
+    {0, 2, 2}, {2, 0, 2}, {1, 2, 2}, {2, 1, 2}, {2, 2, 1}, {2, 2, 2}};
+
+void shapeHost(int t, double const * p, double * phi, double * dphi)
+{
+  double const x = p[0], y = p[1], z = p[2];
+  if (t == P1TET || t == P2TET)
+  {
+    double const l[4] = {1. - x - y - z, x, y, z};
+    double const dl[4][3] = {{-1., -1., -1.}, {1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
+    if (t == P1TET)
+    {
+      for (int i = 0; i < 4; ++i)
+      {
+        phi[i] = l[i];
+        for (int d = 0; d < 3; ++d)
+          dphi[3 * i + d] = dl[i][d];
+      }
+      return;
+    }
+    for (int i = 0; i < 4; ++i)
+    {
+      phi[i] = l[i] * (2. * l[i] - 1.);
+      for (int d = 0; d < 3; ++d)
+        dphi[3 * i + d] = (4. * l[i] - 1.) * dl[i][d];
+    }
+    for (int e = 0; e < 6; ++e)
+    {
+      int const a = tetEdgeV(e, 0), b = tetEdgeV(e, 1);
+      phi[4 + e] = 4. * l[a] * l[b];
+      for (int d = 0; d < 3; ++d)
+        dphi[3 * (4 + e) + d] = 4. * (l[a] * dl[b][d] + dl[a][d] * l[b]);
+    }
+    return;
+  }
+  int const n = (t == Q1HEX) ? 8 : 27;
+  for (int i = 0; i < n; ++i)
+  {
+    int const * ix = (t == Q1HEX) ? kQ1idx[i] : kQ2idx[i];
+    double fx, fy, fz, gx, gy, gz;
+    if (t == Q1HEX)
+    {
+      fx = f1(ix[0], x), fy = f1(ix[1], y), fz = f1(ix[2], z);
+      gx = g1(ix[0], x), gy = g1(ix[1], y), gz = g1(ix[2], z);
+    }
+    else
+    {
+      fx = f2(ix[0], x), fy = f2(ix[1], y), fz = f2(ix[2], z);
+      gx = g2(ix[0], x), gy = g2(ix[1], y), gz = g2(ix[2], z);
+    }
+    phi[i] = fx * fy * fz;
+    dphi[3 * i + 0] = gx * fy * fz;
+    dphi[3 * i + 1] = fx * gy * fz;
+    dphi[3 * i + 2] = fx * fy * gz;
+  }
+}
+
+int gTablesDone[64] = {0};
+} // namespace
+
+pxg_status initTables(pxg_ctx * c)
+{
+  if (c->device >= 0 && c->device < 64 && gTablesDone[c->device])
+    return PXG_OK;
+  for (int t = 0; t < 4; ++t)
+  {
+    std::vector<double> xi, w;
+    ruleHost(t, xi, w);
+    int const nq = (int)w.size(), N = numDofs(t);
+    std::vector<double> phi(nq * N), dphi(nq * N * 3);
+    for (int q = 0; q < nq; ++q)
+      shapeHost(t, &xi[3 * q], &phi[q * N], &dphi[q * N * 3]);
+    if (t == P1TET || t == P2TET)
+    {
+      // reference tensors of the affine elements
+      std::vector<double> T(6 * N * N, 0.), M(N * N, 0.);
+      int const pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+      for (int q = 0; q < nq; ++q)
+        for (int i = 0; i < N; ++i)
+          for (int j = 0; j < N; ++j)
+          {
+            double const * di = &dphi[(q * N + i) * 3];
+            double const * dj = &dphi[(q * N + j) * 3];
+            for (int k = 0; k < 6; ++k)
+            {
+              double v = w[q] * di[pa[k]] * dj[pb[k]];
+              if (k >= 3)
+                v += w[q] * di[pb[k]] * dj[pa[k]];
+              T[(k * N + i) * N + j] += v;
+            }
+            M[i * N + j] += w[q] * phi[q * N + i] * phi[q * N + j];
+          }
+      if (t == P1TET)
+      {
+        std::vector<double> d1(4 * 3);
+        for (int i = 0; i < 12; ++i)
+          d1[i] = dphi[i]; // constant gradients (q = 0)
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1phi, phi.data(), phi.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1dphi, d1.data(), d1.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1w, w.data(), w.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1xi, xi.data(), xi.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1T, T.data(), T.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1M, M.data(), M.size() * 8));
+      }
+      else
+      {
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2phi, phi.data(), phi.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2dphi, dphi.data(), dphi.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2w, w.data(), w.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2xi, xi.data(), xi.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2T, T.data(), T.size() * 8));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2M, M.data(), M.size() * 8));
+      }
+    }
+    else if (t == Q1HEX)
+    {
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ1phi, phi.data(), phi.size() * 8));
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ1dphi, dphi.data(), dphi.size() * 8));
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ1w, w.data(), w.size() * 8));
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ1xi, xi.data(), xi.size() * 8));
+    }
+    else
+    {
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ2phi, phi.data(), phi.size() * 8));
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ2dphi, dphi.data(), dphi.size() * 8));
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ2w, w.data(), w.size() * 8));
+      PXG_CUDA(c, cudaMemcpyToSymbol(cQ2xi, xi.data(), xi.size() * 8));
+    }
+  }
+  if (c->device >= 0 && c->device < 64)
+    gTablesDone[c->device] = 1;
+  return PXG_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+struct LhsDev
+{
+  int on, stiff, mass, bc;
+  double sc, mc;
+  double * vals;
+};
+
+struct AsmArgs
+{
+  int64_t nelem;
+  double const * xyz;
+  uint32_t const * conn;
+  uint32_t const * emap;
+  int32_t const * rowPtr;
+  uint16_t const * rank;
+  double const * kE;
+  uint8_t const * bcMask;
+  double const * bcVal;
+  double bcDiag;
+  LhsDev op[2];
+  int rkind, fn, rbc;
+  double rc;
+  double const * field;
+  double * b;
+};
+
+// adjugate and determinant of a 3x3 matrix
+__device__ __forceinline__ double adj3(double const (&J)[3][3], double (&A)[3][3])
+{
+  A[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  A[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  A[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+  A[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  A[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+  A[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  A[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  A[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  A[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  return J[0][0] * A[0][0] + J[0][1] * A[1][0] + J[0][2] * A[2][0];
+}
+
+// G = s * A A^T (symmetric, packed 00 11 22 01 02 12)
+__device__ __forceinline__ void gram(double const (&A)[3][3], double s, double * G)
+{
+  G[0] = s * (A[0][0] * A[0][0] + A[0][1] * A[0][1] + A[0][2] * A[0][2]);
+  G[1] = s * (A[1][0] * A[1][0] + A[1][1] * A[1][1] + A[1][2] * A[1][2]);
+  G[2] = s * (A[2][0] * A[2][0] + A[2][1] * A[2][1] + A[2][2] * A[2][2]);
+  G[3] = s * (A[0][0] * A[1][0] + A[0][1] * A[1][1] + A[0][2] * A[1][2]);
+  G[4] = s * (A[0][0] * A[2][0] + A[0][1] * A[2][1] + A[0][2] * A[2][2]);
+  G[5] = s * (A[1][0] * A[2][0] + A[1][1] * A[2][1] + A[1][2] * A[2][2]);
+}
+
+__device__ __forceinline__ void red(double * p, double v) { atomicAdd(p, v); }
+
+template <int T>
+__global__ void __launch_bounds__(128) kAssemble(AsmArgs a)
+{
+  constexpr int NV = Elem<T>::NV, N = Elem<T>::N, NQ = Elem<T>::NQ;
+  constexpr bool HEX = Elem<T>::hex;
+  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.nelem)
+    return;
+
+  double X[NV][3];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    uint32_t const id = a.conn[e * NV + v];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      X[v][d] = a.xyz[3 * (int64_t)id + d];
+  }
+  uint32_t dof[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    dof[i] = a.emap[e * N + i];
+  uint32_t cons = 0;
+  if (a.bcMask)
+  {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (a.bcMask[dof[i]])
+        cons |= 1u << i;
+  }
+  double const kfac = a.kE ? a.kE[e] : 1.0;
+  bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
+  bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
+
+  // --- geometry (CurFE::reinit)
+  double G[HEX ? NQ : 1][6];
+  double jxw[NQ];
+  double fq[NQ];
+  double adet = 0.;
+  if constexpr (!HEX)
+  {
+    double J[3][3], A[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        J[r][cc] = X[cc + 1][r] - X[0][r];
+    double const det = adj3(J, A);
+    adet = fabs(det);
+    gram(A, 1.0 / adet, G[0]);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      jxw[q] = adet * WQ<T>(q);
+    if (a.rkind == 1)
+    {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q)
+      {
+        double xq[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          xq[r] = X[0][r] + (J[r][0] * XI<T>(q, 0) + J[r][1] * XI<T>(q, 1) + J[r][2] * XI<T>(q, 2));
+        fq[q] = evalFn(a.fn, a.rc, xq[0], xq[1], xq[2]);
+      }
+    }
+  }
+  else
+  {
+    double P[N][3];
+    mappingPoints<T>(X, P);
+    double o[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      o[d] = .125 * (X[0][d] + X[1][d] + X[2][d] + X[3][d] + X[4][d] + X[5][d] + X[6][d] + X[7][d]);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double J[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}}, A[3][3];
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc)
+            J[r][cc] += P[n][r] * DPHI<T>(q, n, cc);
+      double const det = adj3(J, A);
+      double const ad = fabs(det);
+      gram(A, WQ<T>(q) / ad, G[q]);
+      jxw[q] = WQ<T>(q) * ad;
+      if (a.rkind == 1)
+      {
+        double xq[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          xq[r] = o[r] + (J[r][0] * XI<T>(q, 0) + J[r][1] * XI<T>(q, 1) + J[r][2] * XI<T>(q, 2));
+        fq[q] = evalFn(a.fn, a.rc, xq[0], xq[1], xq[2]);
+      }
+    }
+  }
+  if (a.rkind == 2)
+  {
+    double loc[N];
+#pragma unroll
+    for (int n = 0; n < N; ++n)
+      loc[n] = a.field[dof[n]];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double s = 0.;
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+        s += PHI<T>(q, n) * loc[n];
+      fq[q] = a.rc * s;
+    }
+  }
+
+  // --- local matrices row by row, scattered as they are produced
+  bool const anyBc = cons && ((a.op[0].on && a.op[0].bc) || (a.op[1].on && a.op[1].bc));
+  double lift[2][N];
+  if (anyBc)
+  {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        lift[m][i] = 0.;
+  }
+  int64_t const NN = (int64_t)N * N;
+  uint16_t const * rk = a.rank + e * NN;
+#pragma unroll 1
+  for (int i = 0; i < N; ++i)
+  {
+    int32_t const rpi = a.rowPtr[dof[i]];
+    double v[HEX ? NQ : 1][3];
+    if constexpr (HEX)
+    {
+      if (needK)
+      {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+        {
+          double const d0 = DPHI<T>(q, i, 0), d1 = DPHI<T>(q, i, 1), d2 = DPHI<T>(q, i, 2);
+          v[q][0] = G[q][0] * d0 + G[q][3] * d1 + G[q][4] * d2;
+          v[q][1] = G[q][3] * d0 + G[q][1] * d1 + G[q][5] * d2;
+          v[q][2] = G[q][4] * d0 + G[q][5] * d1 + G[q][2] * d2;
+        }
+      }
+    }
+#pragma unroll 1
+    for (int j = i; j < N; ++j)
+    {
+      double kv = 0., mv = 0.;
+      if constexpr (HEX)
+      {
+        if (needK)
+        {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q)
+            kv += v[q][0] * DPHI<T>(q, j, 0) + v[q][1] * DPHI<T>(q, j, 1) + v[q][2] * DPHI<T>(q, j, 2);
+        }
+        if (needM)
+        {
+#pragma unroll
+          for (int q = 0; q < NQ; ++q)
+            mv += jxw[q] * (PHI<T>(q, i) * PHI<T>(q, j));
+        }
+      }
+      else
+      {
+        if (needK)
+        {
+#pragma unroll
+          for (int k = 0; k < 6; ++k)
+            kv += G[0][k] * TT<T>(k, i, j);
+        }
+        if (needM)
+          mv = adet * MHAT<T>(i, j);
+      }
+      int32_t const pij = rpi + rk[i * N + j];
+      int32_t const pji = a.rowPtr[dof[j]] + rk[j * N + i];
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+      {
+        LhsDev const & op = a.op[m];
+        if (!op.on)
+          continue;
+        double val = 0.;
+        if (op.stiff)
+          val += (op.stiff == 2 ? op.sc * kfac : op.sc) * kv;
+        if (op.mass)
+          val += op.mc * mv;
+        if (op.bc && cons)
+        {
+          bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
+          if (ci || cj)
+          {
+            if (i == j)
+              red(op.vals + pij, a.bcDiag);
+            else
+            {
+              if (!ci)
+                lift[m][i] -= val * a.bcVal[dof[j]];
+              if (!cj)
+                lift[m][j] -= val * a.bcVal[dof[i]];
+            }
+            continue;
+          }
+        }
+        red(op.vals + pij, val);
+        if (j != i)
+          red(op.vals + pji, val);
+      }
+    }
+  }
+  if (a.b)
+  {
+    // BC lifts of the lhs ops (buildLhs: b += C(-Ke h), and h at constrained DOFs)
+    if (anyBc)
+    {
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+      {
+        if (!a.op[m].on || !a.op[m].bc)
+          continue;
+#pragma unroll 1
+        for (int i = 0; i < N; ++i)
+        {
+          double const add = ((cons >> i) & 1u) ? a.bcVal[dof[i]] : lift[m][i];
+          if (add != 0.)
+            red(a.b + dof[i], add);
+        }
+      }
+    }
+    // load vector (buildRhs: b += C Fe)
+    if (a.rkind)
+    {
+#pragma unroll 1
+      for (int i = 0; i < N; ++i)
+      {
+        if (a.rbc && ((cons >> i) & 1u))
+          continue;
+        double fe = 0.;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+          fe += jxw[q] * PHI<T>(q, i) * fq[q];
+        red(a.b + dof[i], fe);
+      }
+    }
+  }
+}
+
+template <int T>
+__global__ void kInterpolate(int64_t nelem, double const * __restrict__ xyz, uint32_t const * __restrict__ conn,
+                             uint32_t const * __restrict__ emap, int fn, double c, double * __restrict__ v)
+{
+  constexpr int NV = Elem<T>::NV, N = Elem<T>::N;
+  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= nelem)
+    return;
+  double X[NV][3], P[N][3];
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+  {
+    uint32_t const id = conn[e * NV + k];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      X[k][d] = xyz[3 * (int64_t)id + d];
+  }
+  mappingPoints<T>(X, P);
+#pragma unroll 1
+  for (int i = 0; i < N; ++i)
+    v[emap[e * N + i]] = evalFn(fn, c, P[i][0], P[i][1], P[i][2]);
+}
+
+// prune(1., 1e-16): an entry is dropped when |v| <= 1e-16 (Eigen's isMuchSmallerThan)
+__device__ __forceinline__ bool pruned(double v) { return fabs(v) <= 1e-16; }
+
+__global__ void kPruneCount(double const * __restrict__ vals, int64_t n, unsigned long long * out)
+{
+  unsigned long long cnt = 0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    cnt += pruned(vals[k]) ? 1ull : 0ull;
+  using WR = cub::WarpReduce<unsigned long long>;
+  __shared__ typename WR::TempStorage ts[8];
+  unsigned long long const s = WR(ts[threadIdx.x / 32]).Sum(cnt);
+  if ((threadIdx.x & 31) == 0 && s)
+    atomicAdd(out, s);
+}
+
+__global__ void kRowKept(int32_t const * __restrict__ rowPtr, double const * __restrict__ vals, int64_t nrows,
+                         int32_t * __restrict__ kept)
+{
+  int64_t const r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrows)
+    return;
+  int32_t k = 0;
+  for (int32_t p = rowPtr[r]; p < rowPtr[r + 1]; ++p)
+    k += pruned(vals[p]) ? 0 : 1;
+  kept[r] = k;
+}
+
+__global__ void kCompact(int32_t const * __restrict__ rowPtr, int32_t const * __restrict__ col,
+                         double const * __restrict__ vals, int64_t nrows, int32_t const * __restrict__ newPtr,
+                         int32_t * __restrict__ colOut, double * __restrict__ valOut)
+{
+  int64_t const r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrows)
+    return;
+  int32_t o = newPtr[r];
+  for (int32_t p = rowPtr[r]; p < rowPtr[r + 1]; ++p)
+    if (!pruned(vals[p]))
+    {
+      colOut[o] = col[p];
+      valOut[o] = vals[p];
+      ++o;
+    }
+}
+
+} // namespace pxg
+
+using namespace pxg;
+
+namespace
+{
+template <int T>
+void launchAssemble(AsmArgs const & a, cudaStream_t s)
+{
+  unsigned const blocks = (unsigned)((a.nelem + 127) / 128);
+  kAssemble<T><<<blocks, 128, 0, s>>>(a);
+}
+} // namespace
+
+extern "C"
+{
+
+pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg_lhs_op const * op1,
+                        double * vals1, pxg_rhs_op const * rhs, double * b, unsigned flags, void * stream)
+{
+  if (!c)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->rowPtr.p)
+    return fail(c, PXG_ERR_INVALID_ARG, "build the pattern first");
+  cudaStream_t const s = (cudaStream_t)stream;
+  AsmArgs a{};
+  a.nelem = c->nelem;
+  a.xyz = c->xyz.p;
+  a.conn = c->conn.p;
+  a.emap = c->emap.p;
+  a.rowPtr = c->rowPtr.p;
+  a.rank = c->rank.p;
+  a.kE = c->hasCoef ? c->kE.p : nullptr;
+  a.bcMask = c->nbc ? c->bcMask.p : nullptr;
+  a.bcVal = c->nbc ? c->bcVal.p : nullptr;
+  a.bcDiag = c->bcDiag;
+  pxg_lhs_op const * ops[2] = {op0, op1};
+  double * outs[2] = {vals0, vals1};
+  bool any = false;
+  for (int m = 0; m < 2; ++m)
+  {
+    if (!ops[m])
+      continue;
+    pxg_lhs_op const & o = *ops[m];
+    if (o.stiffness < 0 || o.stiffness > 2 || o.mass < 0 || o.mass > 1)
+      return fail(c, PXG_ERR_INVALID_ARG, "lhs op %d: bad stiffness/mass kind", m);
+    if (!outs[m])
+      return fail(c, PXG_ERR_INVALID_ARG, "lhs op %d has no output array", m);
+    if (o.stiffness == 2 && !c->hasCoef)
+      return fail(c, PXG_ERR_INVALID_ARG, "lhs op %d needs the per-element coefficient (pxg_set_coef)", m);
+    a.op[m] = LhsDev{1, o.stiffness, o.mass, o.apply_bc, o.stiff_coef, o.mass_coef, outs[m]};
+    any = true;
+  }
+  if (rhs && rhs->kind)
+  {
+    if (rhs->kind < 0 || rhs->kind > 2)
+      return fail(c, PXG_ERR_INVALID_ARG, "rhs kind %d", rhs->kind);
+    if (rhs->kind == 1 && (rhs->fn < 0 || rhs->fn > PXG_FN_POISSON_EXACT))
+      return fail(c, PXG_ERR_INVALID_ARG, "unknown analytic function %d", rhs->fn);
+    if (rhs->kind == 2 && !rhs->field)
+      return fail(c, PXG_ERR_INVALID_ARG, "projection needs a field");
+    if (!b)
+      return fail(c, PXG_ERR_INVALID_ARG, "rhs op has no output vector");
+    a.rkind = rhs->kind;
+    a.fn = rhs->fn;
+    a.rc = rhs->coef;
+    a.field = rhs->field;
+    a.rbc = rhs->apply_bc;
+    any = true;
+  }
+  a.b = b;
+  if (!any)
+    return PXG_OK;
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  if (!(flags & PXG_ACCUMULATE))
+  {
+    for (int m = 0; m < 2; ++m)
+      if (a.op[m].on)
+        PXG_CUDA(c, cudaMemsetAsync(a.op[m].vals, 0, (size_t)c->nnz * 8, s));
+    if (b)
+      PXG_CUDA(c, cudaMemsetAsync(b, 0, (size_t)c->ndof * 8, s));
+  }
+  switch (c->etype)
+  {
+  case P1TET:
+    launchAssemble<P1TET>(a, s);
+    break;
+  case P2TET:
+    launchAssemble<P2TET>(a, s);
+    break;
+  case Q1HEX:
+    launchAssemble<Q1HEX>(a, s);
+    break;
+  case Q2HEX:
+    launchAssemble<Q2HEX>(a, s);
+    break;
+  }
+  PXG_CUDA(c, cudaGetLastError());
+  return PXG_OK;
+}
+
+pxg_status pxg_prune_count(pxg_ctx * c, double const * vals, int64_t * pruned, void * stream)
+{
+  if (!c || !vals || !pruned)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->rowPtr.p)
+    return fail(c, PXG_ERR_INVALID_ARG, "no pattern built");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  PXG_CUDA(c, cudaMemsetAsync(c->counter.p, 0, 8, s));
+  kPruneCount<<<152 * 8, 256, 0, s>>>(vals, c->nnz, c->counter.p);
+  PXG_CUDA(c, cudaGetLastError());
+  unsigned long long h = 0;
+  PXG_CUDA(c, cudaMemcpyAsync(&h, c->counter.p, 8, cudaMemcpyDeviceToHost, s));
+  PXG_CUDA(c, cudaStreamSynchronize(s));
+  *pruned = (int64_t)h;
+  return PXG_OK;
+}
+
+pxg_status pxg_close_matrix(pxg_ctx * c, double const * vals, int32_t * rp, int32_t * ci, double * vout,
+                            int64_t * nnzOut, void * stream)
+{
+  if (!c || !vals || !rp || !ci || !vout || !nnzOut)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->rowPtr.p)
+    return fail(c, PXG_ERR_INVALID_ARG, "no pattern built");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  int64_t const n = c->ndof;
+  DevBuf<int32_t> kept;
+  PXG_CUDA(c, kept.alloc(n + 1));
+  unsigned const blocks = (unsigned)((n + 255) / 256);
+  kRowKept<<<blocks, 256, 0, s>>>(c->rowPtr.p, vals, n, kept.p);
+  PXG_CUDA(c, cudaMemsetAsync(kept.p + n, 0, 4, s));
+  size_t tb = 0;
+  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(nullptr, tb, kept.p, rp, n + 1, s));
+  DevBuf<unsigned char> tmp;
+  PXG_CUDA(c, tmp.alloc(tb));
+  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, tb, kept.p, rp, n + 1, s));
+  kCompact<<<blocks, 256, 0, s>>>(c->rowPtr.p, c->colIdx.p, vals, n, rp, ci, vout);
+  PXG_CUDA(c, cudaGetLastError());
+  int32_t tot = 0;
+  PXG_CUDA(c, cudaMemcpyAsync(&tot, rp + n, 4, cudaMemcpyDeviceToHost, s));
+  PXG_CUDA(c, cudaStreamSynchronize(s));
+  *nnzOut = tot;
+  return PXG_OK;
+}
+
+pxg_status pxg_interpolate(pxg_ctx * c, int fn, double coef, double * v, void * stream)
+{
+  if (!c || !v)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->emap.p)
+    return fail(c, PXG_ERR_INVALID_ARG, "no DOF map");
+  if (fn < 0 || fn > PXG_FN_POISSON_EXACT)
+    return fail(c, PXG_ERR_INVALID_ARG, "unknown analytic function %d", fn);
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  unsigned const blocks = (unsigned)((c->nelem + 127) / 128);
+  switch (c->etype)
+  {
+  case P1TET:
+    kInterpolate<P1TET><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, c->emap.p, fn, coef, v);
+    break;
+  case P2TET:
+    kInterpolate<P2TET><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, c->emap.p, fn, coef, v);
+    break;
+  case Q1HEX:
+    kInterpolate<Q1HEX><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, c->emap.p, fn, coef, v);
+    break;
+  case Q2HEX:
+    kInterpolate<Q2HEX><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, c->emap.p, fn, coef, v);
+    break;
+  }
+  PXG_CUDA(c, cudaGetLastError());
+  return PXG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,231 @@
+// Internal declarations of the GB300 assembly engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <utility>
+
+#include "../../include/pxg.h"
+
+namespace pxg
+{
+
+enum : int
+{
+  P1TET = 0,
+  P2TET = 1,
+  Q1HEX = 2,
+  Q2HEX = 3,
+};
+
+// Element traits: vertices, DOFs, quadrature points (LagrangeFE<...>::RecommendedQR,
+// include/fe.hpp:96-131 of proxpde).
+template <int T>
+struct Elem;
+template <>
+struct Elem<P1TET>
+{
+  static constexpr int NV = 4, N = 4, NQ = 4;
+  static constexpr bool hex = false;
+};
+template <>
+struct Elem<P2TET>
+{
+  static constexpr int NV = 4, N = 10, NQ = 11;
+  static constexpr bool hex = false;
+};
+template <>
+struct Elem<Q1HEX>
+{
+  static constexpr int NV = 8, N = 8, NQ = 8;
+  static constexpr bool hex = true;
+};
+template <>
+struct Elem<Q2HEX>
+{
+  static constexpr int NV = 8, N = 27, NQ = 27;
+  static constexpr bool hex = true;
+};
+
+inline int numVerts(int t) { return (t == P1TET || t == P2TET) ? 4 : 8; }
+inline int numDofs(int t) { return t == P1TET ? 4 : t == P2TET ? 10 : t == Q1HEX ? 8 : 27; }
+inline int numQpts(int t) { return t == P1TET ? 4 : t == P2TET ? 11 : t == Q1HEX ? 8 : 27; }
+inline bool isHex(int t) { return t == Q1HEX || t == Q2HEX; }
+
+// Local topology (include/geo.hpp:520-529, 640-665 of proxpde).
+__host__ __device__ constexpr int tetEdgeV(int e, int k)
+{
+  constexpr int t[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+  return t[e][k];
+}
+__host__ __device__ constexpr int hexEdgeV(int e, int k)
+{
+  constexpr int t[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {0, 4}, {1, 5},
+                            {2, 6}, {3, 7}, {4, 5}, {5, 6}, {6, 7}, {7, 4}};
+  return t[e][k];
+}
+__host__ __device__ constexpr int hexFaceV(int f, int k)
+{
+  constexpr int t[6][4] = {{0, 3, 2, 1}, {3, 0, 4, 7}, {0, 1, 5, 4},
+                           {1, 2, 6, 5}, {2, 3, 7, 6}, {4, 5, 6, 7}};
+  return t[f][k];
+}
+
+// Mapping points = DOF points of the Lagrange elements, built from the vertices
+// (RefFE::dofPts / mappingPts, include/reffe.hpp:748-767, 960-988 of proxpde).
+template <int T>
+__host__ __device__ inline void mappingPoints(double const (*X)[3], double (*P)[3])
+{
+  constexpr int NV = Elem<T>::NV;
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      P[v][d] = X[v][d];
+  if constexpr (T == P2TET)
+  {
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        P[4 + e][d] = .5 * (X[tetEdgeV(e, 0)][d] + X[tetEdgeV(e, 1)][d]);
+  }
+  if constexpr (T == Q2HEX)
+  {
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        P[8 + e][d] = 0.5 * (X[hexEdgeV(e, 0)][d] + X[hexEdgeV(e, 1)][d]);
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        P[20 + f][d] = 0.25 * (X[hexFaceV(f, 0)][d] + X[hexFaceV(f, 1)][d] +
+                               X[hexFaceV(f, 2)][d] + X[hexFaceV(f, 3)][d]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      P[26][d] = .125 * (X[0][d] + X[1][d] + X[2][d] + X[3][d] + X[4][d] + X[5][d] +
+                         X[6][d] + X[7][d]);
+  }
+}
+
+// Analytic functions by id (pxg_fn).  sinpi(x) is sin(pi x) without the rounding of
+// pi x; it agrees with the reference's std::sin(M_PI * x) to round-off.
+__host__ __device__ inline double evalFn(int fn, double c, double x, double y, double z)
+{
+#ifdef __CUDA_ARCH__
+  switch (fn)
+  {
+  case PXG_FN_CONST:
+    return c;
+  case PXG_FN_SIN3:
+    return c * (sinpi(x) * sinpi(y) * sinpi(z));
+  case PXG_FN_POISSON_RHS:
+    return c * (2.5 * 3.141592653589793 * 3.141592653589793 * sinpi(0.5 * x) * sinpi(1.5 * y));
+  case PXG_FN_POISSON_EXACT:
+    return c * (sinpi(0.5 * x) * sinpi(1.5 * y));
+  }
+  return __longlong_as_double(0x7ff8000000000000ll);
+#else
+  (void)fn;
+  (void)c;
+  (void)x;
+  (void)y;
+  (void)z;
+  return 0.0;
+#endif
+}
+
+// ------------------------------------------------------------ device buffer
+template <typename T>
+struct DevBuf
+{
+  T * p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(DevBuf const &) = delete;
+  DevBuf & operator=(DevBuf const &) = delete;
+  ~DevBuf() { reset(); }
+  void reset()
+  {
+    if (p)
+      cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count)
+  {
+    reset();
+    if (count == 0)
+      return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess)
+    {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+} // namespace pxg
+
+// ----------------------------------------------------------------- context
+struct pxg_ctx
+{
+  int device = 0;
+  std::string err;
+  // mesh
+  int etype = -1;
+  int nv = 0, N = 0;
+  int64_t nnodes = 0, nelem = 0;
+  pxg::DevBuf<double> xyz;
+  pxg::DevBuf<uint32_t> conn;
+  // DOF map
+  int64_t ndof = 0;
+  pxg::DevBuf<uint32_t> emap;
+  // structural pattern + per-element scatter ranks (rank[e][i][j]: position of
+  // column emap[e][j] inside row emap[e][i])
+  int64_t nnz = 0;
+  int maxRowLen = 0;
+  pxg::DevBuf<int32_t> rowPtr, colIdx;
+  pxg::DevBuf<uint16_t> rank;
+  // coefficient and BCs
+  pxg::DevBuf<double> kE;
+  bool hasCoef = false;
+  pxg::DevBuf<uint8_t> bcMask;
+  pxg::DevBuf<double> bcVal;
+  int64_t nbc = 0;
+  double bcDiag = 1.0;
+  // small device scratch (counters, flags)
+  pxg::DevBuf<unsigned long long> counter;
+};
+
+// status helpers shared by the translation units
+namespace pxg
+{
+pxg_status fail(pxg_ctx * c, pxg_status s, char const * fmt, ...);
+pxg_status cudaFail(pxg_ctx * c, cudaError_t e, char const * what);
+pxg_status ensureDevice(pxg_ctx * c);
+
+// pattern / dofmap (pxg_pattern.cu)
+pxg_status buildDofmap(pxg_ctx * c);
+pxg_status buildPattern(pxg_ctx * c);
+
+// reference tables (pxg_assemble.cu)
+pxg_status initTables(pxg_ctx * c);
+} // namespace pxg
+
+#define PXG_CUDA(ctx, call)                                                                    \
+  do                                                                                           \
+  {                                                                                            \
+    cudaError_t _e = (call);                                                                   \
+    if (_e != cudaSuccess)                                                                     \
+      return pxg::cudaFail((ctx), _e, #call);                                                  \
+  } while (0)

@@ -1,0 +1,116 @@
+"""Shared helpers of the tests: synthetic problems, the engine path through the C ABI,
+the oracle path, and the comparison rules.
+
+Tolerance (values): |v_gpu - v_oracle| <= 1e-12 * max|v_oracle| for every entry of a
+matrix or vector (normwise relative, FP64 on both sides, different summation
+order); the CSR pattern (row_ptr, col_idx) and the DOF map must be identical.
+"""
+import numpy as np
+
+import oracle as O
+from proxpde_gb300 import meshgen
+
+TOL = 1e-12
+GEN = {"hex": meshgen.cube_hex, "tet5": meshgen.cube_tet5, "tet6": meshgen.cube_tet6}
+
+
+def problem(gen, n, alpha=0.0, seed=1, sigma=None):
+    xyz, conn = GEN[gen](n)
+    if alpha:
+        xyz = meshgen.perturb(xyz, n, alpha, seed)
+    k = meshgen.lognormal(seed + 1, conn.shape[0], sigma) if sigma else None
+    return xyz, conn, k
+
+
+def gpu_assemble(t, xyz, conn, ops, rhs=None, k=None, bc=None, device=0, field=None):
+    """Run the engine through the C ABI. ops: list of up to two lhs op dicts.
+    Returns dict(em, ndof, pattern, mats=[(rp, col, val)], b)."""
+    import torch
+
+    from proxpde_gb300 import Context
+
+    ctx = Context(device)
+    ctx.set_mesh(t, xyz, conn)
+    ndof = ctx.build_dofmap()
+    nnz = ctx.build_pattern()
+    if k is not None:
+        ctx.set_coef(np.ascontiguousarray(k))
+    if bc is not None:
+        dofs, vals = bc
+        ctx.set_bc(dofs, vals, 1.0)
+    dev = f"cuda:{device}"
+    vals = [torch.empty(nnz, dtype=torch.float64, device=dev) for _ in ops]
+    b = torch.empty(ndof, dtype=torch.float64, device=dev)
+    if rhs is not None and rhs.get("kind") == 2:
+        rhs = dict(rhs)
+        rhs["field"] = torch.as_tensor(field).to(dev)
+    ctx.assemble(op0=ops[0] if ops else None, vals0=vals[0] if ops else None,
+                 op1=ops[1] if len(ops) > 1 else None, vals1=vals[1] if len(ops) > 1 else None,
+                 rhs=rhs, b=b)
+    mats = []
+    for v in vals:
+        rp = torch.empty(ndof + 1, dtype=torch.int32, device=dev)
+        ci = torch.empty(nnz, dtype=torch.int32, device=dev)
+        vo = torch.empty(nnz, dtype=torch.float64, device=dev)
+        m = ctx.close_matrix(v, rp, ci, vo)
+        mats.append((rp.cpu().numpy(), ci[:m].cpu().numpy(), vo[:m].cpu().numpy()))
+    torch.cuda.synchronize()
+    out = dict(ndof=ndof, nnz=nnz, em=ctx.get_dofmap(), pattern=ctx.get_pattern(), mats=mats, b=b.cpu().numpy(),
+               ctx=ctx, struct_vals=[v.cpu().numpy() for v in vals])
+    return out
+
+
+def oracle_lhs(op, k):
+    d = {"stiff_kind": op.get("stiffness", 0), "stiff_c": op.get("stiff_coef", 1.0), "mass_kind": op.get("mass", 0),
+         "mass_c": op.get("mass_coef", 1.0), "apply_bc": op.get("apply_bc", 0)}
+    if d["stiff_kind"] == 2:
+        d["k_e"] = np.asarray(k) * op.get("stiff_coef", 1.0)
+    return d
+
+
+def structural_pattern(em, ndof):
+    keys = np.unique((em[:, :, None].astype(np.int64) * ndof + em[:, None, :]).reshape(-1))
+    rows, cols = keys // ndof, keys % ndof
+    rp = np.zeros(ndof + 1, dtype=np.int64)
+    np.add.at(rp, rows + 1, 1)
+    return np.cumsum(rp).astype(np.int32), cols.astype(np.int32)
+
+
+def assert_close(a, b, tol=TOL, what=""):
+    scale = max(np.abs(b).max(), 1e-300)
+    err = np.abs(a - b).max() if a.size else 0.0
+    assert err <= tol * scale, f"{what}: max|diff| {err:.3e} > {tol:g} * {scale:.3e}"
+    return err / scale
+
+
+ROUNDOFF_BAND = 64 * 2.220446049250313e-16
+
+
+def compare_csr(g, o, ndof, tol=TOL):
+    """Compare a pruned engine CSR with the oracle's.
+
+    Values: normwise 1e-12.  Pattern: identical, except entries that are present on
+    one side only AND whose value there is round-off (|v| <= 64 eps * max|row|):
+    such entries are mathematically zero, and whether they clear closeMatrix's
+    1e-16 prune threshold depends on evaluation order in the reference as well.
+    Returns the number of such round-off entries."""
+    import scipy.sparse as sp
+
+    A = sp.csr_matrix((g[2], g[1], g[0]), shape=(ndof, ndof))
+    B = sp.csr_matrix((o[2], o[1], o[0]), shape=(ndof, ndof))
+    scale = np.abs(o[2]).max()
+    D = (A - B).tocoo()
+    err = np.abs(D.data).max() if D.nnz else 0.0
+    assert err <= tol * scale, f"values: max|diff| {err:.3e} > {tol:g} * {scale:.3e}"
+    if np.array_equal(g[0], o[0]) and np.array_equal(g[1], o[1]):
+        return 0
+    Pa = sp.csr_matrix((np.ones(g[1].size), g[1], g[0]), shape=(ndof, ndof))
+    Pb = sp.csr_matrix((np.ones(o[1].size), o[1], o[0]), shape=(ndof, ndof))
+    only = (Pa - Pb).tocoo()
+    rowmax = np.maximum(np.abs(A).max(axis=1).toarray().ravel(), np.abs(B).max(axis=1).toarray().ravel())
+    n_band = 0
+    for r, c, s in zip(only.row, only.col, only.data):
+        v = A[r, c] if s > 0 else B[r, c]
+        assert abs(v) <= ROUNDOFF_BAND * rowmax[r], f"pattern differs at ({r},{c}) with |v|={abs(v):.3e}"
+        n_band += 1
+    return n_band

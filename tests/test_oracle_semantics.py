@@ -1,0 +1,88 @@
+"""Builder semantics the oracle restates (include/builder.hpp), checked on small
+cases: duplicate summation and prune at closeMatrix, BC condensation with
+multiplicity on the diagonal, first-touch DOF numbering, serial == OpenMP."""
+import numpy as np
+import pytest
+
+import oracle as O
+from proxpde_gb300 import meshgen
+
+
+def test_mesh_builders_match_reference_restatement(oracle_lib):
+    for n in (1, 2, 5):
+        a = O.cube_hex(n)
+        b = meshgen.cube_hex(n)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        a = O.cube_tet5(n)
+        b = meshgen.cube_tet5(n)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_kuhn_split_volume():
+    xyz, conn = meshgen.cube_tet6(3)
+    X = xyz[conn.astype(np.int64)]
+    v = np.abs(np.einsum("ij,ij->i", np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]), X[:, 3] - X[:, 0])) / 6
+    assert abs(v.sum() - 1.0) < 1e-14 and np.all(v > 0)
+
+
+def test_first_touch_numbering_hex(oracle_lib):
+    # element 0 = nodes (0,1,2+n,1+n, ...) gets DOFs 0..7 in its local order
+    xyz, conn = O.cube_hex(2)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    assert ndof == 27
+    assert list(em[0]) == list(range(8))
+    # element 1 shares 4 nodes with element 0 and creates 4 new DOFs 8..11
+    assert sorted(set(em[1]) - set(em[0])) == [8, 9, 10, 11]
+
+
+@pytest.mark.parametrize("t", [O.P2TET, O.Q2HEX])
+def test_first_touch_interleaves_entities(oracle_lib, t):
+    gen = O.cube_tet5 if t == O.P2TET else O.cube_hex
+    xyz, conn = gen(2)
+    em, ndof = O.dofmap(t, xyz.shape[0], conn)
+    assert list(em[0]) == list(range(O.num_dofs(t)))
+    assert em.max() + 1 == ndof and len(np.unique(em)) == ndof
+
+
+def test_prune_and_duplicate_sum(oracle_lib):
+    # unperturbed Q1 stiffness with k=1: face-neighbour entries cancel exactly and
+    # are pruned; every other structural entry survives
+    xyz, conn = O.cube_hex(3)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    csr, _ = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs={"stiff_kind": 1, "stiff_c": 1.0})
+    rp, col, val = csr
+    assert np.all(np.abs(val) > 1e-16)
+    keys = np.unique(em[:, :, None].astype(np.int64) * ndof + em[:, None, :])
+    assert len(keys) > len(val)  # some structural entries were pruned
+    A = O.csr_to_scipy(csr, ndof)
+    assert abs(A - A.T).max() < 1e-15
+    assert np.abs(A @ np.ones(ndof)).max() < 1e-14  # constants are in the kernel
+
+
+def test_bc_diagonal_multiplicity(oracle_lib):
+    xyz, conn = O.cube_hex(2)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    dx = O.dof_coords(O.Q1HEX, xyz, conn, em, ndof)
+    mask = O.plane_bc_mask(dx, [("x", 0.0)])
+    csr, b = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs={"stiff_kind": 1, "stiff_c": 1.0, "apply_bc": 1},
+                     bc_mask=mask, bc_val=np.full(ndof, 2.0))
+    A = O.csr_to_scipy(csr, ndof).toarray()
+    mult = np.bincount(em.reshape(-1), minlength=ndof)
+    for d in np.nonzero(mask)[0]:
+        assert A[d, d] == mult[d]  # diag = 1.0 once per touching element
+        assert np.count_nonzero(A[d]) == 1 and np.count_nonzero(A[:, d]) == 1
+        assert b[d] == 2.0 * mult[d]
+
+
+def test_openmp_equals_serial(oracle_lib):
+    xyz, conn = meshgen.cube_tet6(4)
+    xyz = meshgen.perturb(xyz, 4, 0.2, 7)
+    k = meshgen.lognormal(8, conn.shape[0])
+    em, ndof = O.dofmap(O.P1TET, xyz.shape[0], conn)
+    lhs = {"stiff_kind": 2, "k_e": k, "mass_kind": 1, "mass_c": 1.0}
+    rhs = {"kind": 1, "fn": O.FN_SIN3, "c": 1.0}
+    a, ba = O.build(O.P1TET, xyz, conn, em, ndof, lhs=lhs, rhs=rhs, nthreads=1)
+    b, bb = O.build(O.P1TET, xyz, conn, em, ndof, lhs=lhs, rhs=rhs, nthreads=4)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert np.array_equal(ba, bb)
