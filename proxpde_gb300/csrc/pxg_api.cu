@@ -1,6 +1,7 @@
 // Context lifecycle, inputs (mesh, DOF map, coefficient, BCs) and outputs of the
 // C ABI declared in include/pxg.h.
 #include <cstdarg>
+#include <cstdlib>
 #include <vector>
 
 #include "pxg_internal.h"
@@ -118,6 +119,8 @@ pxg_status pxg_create(pxg_ctx ** out, int device)
     return PXG_ERR_NO_DEVICE;
   auto * c = new pxg_ctx;
   c->device = device;
+  char const * gen = getenv("PXG_Q1_GENERIC");
+  c->q1Generic = gen && gen[0] == '1';
   pxg_status s = ensureDevice(c);
   if (s == PXG_OK)
     s = initTables(c);

@@ -300,32 +300,6 @@ pxg_status initTables(pxg_ctx * c)
 }
 
 // ------------------------------------------------------------------ kernels
-struct LhsDev
-{
-  int on, stiff, mass, bc;
-  double sc, mc;
-  double * vals;
-};
-
-struct AsmArgs
-{
-  int64_t nelem;
-  double const * xyz;
-  uint32_t const * conn;
-  uint32_t const * emap;
-  int32_t const * rowPtr;
-  uint16_t const * rank;
-  double const * kE;
-  uint8_t const * bcMask;
-  double const * bcVal;
-  double bcDiag;
-  LhsDev op[2];
-  int rkind, fn, rbc;
-  double rc;
-  double const * field;
-  double * b;
-};
-
 // adjugate and determinant of a 3x3 matrix
 __device__ __forceinline__ double adj3(double const (&J)[3][3], double (&A)[3][3])
 {
@@ -765,7 +739,10 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     launchAssemble<P2TET>(a, s);
     break;
   case Q1HEX:
-    launchAssemble<Q1HEX>(a, s);
+    if (c->q1Generic)
+      launchAssemble<Q1HEX>(a, s);
+    else
+      launchAssembleQ1(a, s);
     break;
   case Q2HEX:
     launchAssemble<Q2HEX>(a, s);

@@ -205,7 +205,41 @@ struct pxg_ctx
   double bcDiag = 1.0;
   // small device scratch (counters, flags)
   pxg::DevBuf<unsigned long long> counter;
+  // PXG_Q1_GENERIC=1 in the environment selects the generic kernel for Q1 hexahedra
+  bool q1Generic = false;
 };
+
+// arguments of the element kernels
+namespace pxg
+{
+struct LhsDev
+{
+  int on, stiff, mass, bc;
+  double sc, mc;
+  double * vals;
+};
+
+struct AsmArgs
+{
+  int64_t nelem;
+  double const * xyz;
+  uint32_t const * conn;
+  uint32_t const * emap;
+  int32_t const * rowPtr;
+  uint16_t const * rank;
+  double const * kE;
+  uint8_t const * bcMask;
+  double const * bcVal;
+  double bcDiag;
+  LhsDev op[2];
+  int rkind, fn, rbc;
+  double rc;
+  double const * field;
+  double * b;
+};
+
+void launchAssembleQ1(AsmArgs const & a, cudaStream_t s);
+} // namespace pxg
 
 // status helpers shared by the translation units
 namespace pxg

@@ -174,9 +174,10 @@ __global__ void kCsrFromKeys(uint64_t const * __restrict__ ukeys, int64_t nnz, u
 __global__ void kMaxRowLen(int32_t const * __restrict__ rowPtr, int64_t n, unsigned long long * out)
 {
   int64_t const r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n)
-    return;
-  atomicMax(out, (unsigned long long)(rowPtr[r + 1] - rowPtr[r]));
+  unsigned const len = (r < n) ? (unsigned)(rowPtr[r + 1] - rowPtr[r]) : 0u;
+  unsigned const m = __reduce_max_sync(0xffffffffu, len);
+  if ((threadIdx.x & 31) == 0 && m)
+    atomicMax(out, (unsigned long long)m);
 }
 
 __global__ void kRank(uint32_t const * __restrict__ emap, int64_t nelem, int N,
