@@ -182,6 +182,26 @@ pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_pt
  * (interpolateAnalyticFunction, include/fespace.hpp:195-271): v[ndof], device. */
 pxg_status pxg_interpolate(pxg_ctx * ctx, int fn, double coef, double * v, void * stream);
 
+/* ----------------------------------------------------- allocation-free prune
+ * No counterpart in proxpde: an allocation-free variant of pxg_close_matrix's
+ * prune/compact for callers that cannot call cudaMalloc (code running where the
+ * host application owns every device allocation, or where driver allocations are
+ * forbidden, such as host callbacks and real-time sections).  It needs no context:
+ * the caller passes the structural CSR (row_ptr[nrows+1], col_idx, vals) and the
+ * outputs (row_ptr_out[nrows+1], col_idx_out and vals_out with the input's
+ * capacity), all device pointers on the current device, and gets the kept-entry
+ * count in *nnz_out (host).  Entries with |v| <= 1e-16 are dropped, as
+ * Builder::closeMatrix's prune(1., 1e-16) does.
+ * Limits: nrows <= 4,194,304 (else PXG_ERR_INVALID_ARG); its intermediate data live
+ * in one fixed 16.8 MB device array that every GPU loading the library keeps until
+ * exit.  The first call on a device looks up that array's address (make it before
+ * any stream capture).  Calls that overlap on the GPU share the array and race:
+ * serialise them.  It synchronises `stream` to return the count. */
+pxg_status pxg_prune_csr_noalloc(const int32_t * row_ptr, const int32_t * col_idx,
+                                 const double * vals, int64_t nrows, int32_t * row_ptr_out,
+                                 int32_t * col_idx_out, double * vals_out, int64_t * nnz_out,
+                                 void * stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,7 @@ EXPORTS = [
     "pxg_create", "pxg_destroy", "pxg_last_error", "pxg_status_string", "pxg_version",
     "pxg_set_mesh", "pxg_set_coords", "pxg_build_dofmap", "pxg_set_dofmap", "pxg_get_dofmap",
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
-    "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate",
+    "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
 ]
 
 
@@ -90,6 +90,7 @@ def load(path: str = LIB_PATH):
         "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
         "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_interpolate": ([vp, C.c_int, C.c_double, vp, vp], C.c_int),
+        "pxg_prune_csr_noalloc": ([vp, vp, vp, i64, vp, vp, vp, i64p, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -1,0 +1,66 @@
+"""The allocation-free prune entry point (pxg_prune_csr_noalloc) against the regular
+closeMatrix entry point (pxg_close_matrix), through the C ABI.
+
+The entry point exists for callers that cannot allocate GPU memory (for example a
+host application that owns every device allocation, or code running in a host
+callback); it keeps its intermediate data in a fixed device array instead.  Two
+calls in a row must both reproduce the regular entry point exactly: the second call
+finds the array holding the first call's data and must not depend on it.
+
+This file is named to be collected last, so that a failure here does not hide the
+results of the other tests in a run that stops at the first failure.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_prune_matches_close_matrix(engine):
+    import torch
+
+    from proxpde_gb300 import Context, _lib, meshgen
+
+    # unperturbed P1 mesh with k = 1: many stiffness sums cancel and are pruned
+    xyz, conn = meshgen.cube_tet6(10)
+    ctx = Context(0)
+    ctx.set_mesh(_lib.P1TET, xyz, conn)
+    ndof = ctx.build_dofmap()
+    nnz = ctx.build_pattern()
+    vals = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    ctx.assemble(op0={"stiffness": 1, "stiff_coef": 1.0}, vals0=vals)
+
+    # regular entry point
+    rp = torch.empty(ndof + 1, dtype=torch.int32, device="cuda")
+    ci = torch.empty(nnz, dtype=torch.int32, device="cuda")
+    vo = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    m = ctx.close_matrix(vals, rp, ci, vo)
+    assert 0 < m < nnz
+    ref = (rp.cpu().numpy(), ci[:m].cpu().numpy(), vo[:m].cpu().numpy())
+
+    L = _lib.load()
+    srp, sci = ctx.pattern_device()
+    for call in range(2):
+        rp2 = torch.full((ndof + 1,), -7, dtype=torch.int32, device="cuda")
+        ci2 = torch.full((nnz,), -7, dtype=torch.int32, device="cuda")
+        vo2 = torch.full((nnz,), np.nan, dtype=torch.float64, device="cuda")
+        n_out = C.c_int64(-1)
+        st = L.pxg_prune_csr_noalloc(srp, sci, vals.data_ptr(), ndof, rp2.data_ptr(), ci2.data_ptr(),
+                                     vo2.data_ptr(), C.byref(n_out), None)
+        assert st == 0, f"call {call}: status {st}"
+        assert n_out.value == m
+        torch.cuda.synchronize()
+        assert np.array_equal(rp2.cpu().numpy(), ref[0])
+        assert np.array_equal(ci2[:m].cpu().numpy(), ref[1])
+        assert np.array_equal(vo2[:m].cpu().numpy(), ref[2])  # a pure compaction: exact
+
+
+def test_noalloc_rejects_oversize(engine):
+    from proxpde_gb300 import _lib
+
+    L = _lib.load()
+    n_out = C.c_int64(-1)
+    st = L.pxg_prune_csr_noalloc(1, 1, 1, (1 << 22) + 1, 1, 1, 1, C.byref(n_out), None)
+    assert st == 1 and n_out.value == -1
