@@ -182,6 +182,32 @@ pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_pt
  * (interpolateAnalyticFunction, include/fespace.hpp:195-271): v[ndof], device. */
 pxg_status pxg_interpolate(pxg_ctx * ctx, int fn, double coef, double * v, void * stream);
 
+/* ------------------------------------------------------- solve and adjoint
+ * Jacobi-preconditioned CG on a device CSR matrix (symmetric positive definite):
+ * x = A^-1 b to ||b - A x|| <= rtol ||b|| within max_iter iterations, x starting at 0.
+ * proxpde solves with UmfPackLU (include/sparse_matrix.hpp:44, include/solver.hpp:65);
+ * this plain device CG is the engine's solver.  Returns PXG_ERR_NOT_CONVERGED (x holds
+ * the last iterate) when the tolerance is not met. */
+pxg_status pxg_cg(pxg_ctx * ctx, const int32_t * row_ptr, const int32_t * col_idx,
+                  const double * vals, int64_t n, const double * b, double * x, double rtol,
+                  int max_iter, int * iters, double * rel_res, void * stream);
+/* Adjoint gradient with respect to log k_e of a loss J(u) with K(k) u = b:
+ * grad[e] = -(C u)_e^T K_e (C lambda)_e, K_e = k_e K0_e the element stiffness of the
+ * context's coefficient (AssemblyStiffnessFE), C zeroing the DOFs of the essential BCs;
+ * lambda solves K lambda = dJ/du.  u, lambda: device, ndof; grad: device, nelem. */
+pxg_status pxg_adjoint_grad(pxg_ctx * ctx, const double * u, const double * lambda, double * grad,
+                            void * stream);
+/* Forward/backward operator pair (the shape of a torch.autograd.Function):
+ * forward assembles K(k) (with BCs), M and b (from `rhs`, with BCs), solves K u = b by
+ * CG, and returns J = 1/2 (u - u_target)^T M (u - u_target); it keeps K, M, u and
+ * M (u - u_target) in the context.  backward solves K lambda = M (u - u_target) and
+ * writes grad[e] = dloss * dJ/dlog k_e (and lambda if lambda_out is not NULL). */
+pxg_status pxg_adjoint_forward(pxg_ctx * ctx, const pxg_rhs_op * rhs, const double * u_target,
+                               double rtol, int max_iter, double * u_out, double * loss, int * iters,
+                               void * stream);
+pxg_status pxg_adjoint_backward(pxg_ctx * ctx, double dloss, double * grad, double * lambda_out,
+                                int * iters, void * stream);
+
 /* ----------------------------------------------------- allocation-free prune
  * No counterpart in proxpde: an allocation-free variant of pxg_close_matrix's
  * prune/compact for callers that cannot call cudaMalloc (code running where the

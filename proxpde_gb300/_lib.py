@@ -28,6 +28,7 @@ EXPORTS = [
     "pxg_set_mesh", "pxg_set_coords", "pxg_build_dofmap", "pxg_set_dofmap", "pxg_get_dofmap",
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
     "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
+    "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
 ]
 
 
@@ -91,6 +92,12 @@ def load(path: str = LIB_PATH):
         "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_interpolate": ([vp, C.c_int, C.c_double, vp, vp], C.c_int),
         "pxg_prune_csr_noalloc": ([vp, vp, vp, i64, vp, vp, vp, i64p, vp], C.c_int),
+        "pxg_cg": ([vp, vp, vp, vp, i64, vp, vp, C.c_double, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp],
+                   C.c_int),
+        "pxg_adjoint_grad": ([vp, vp, vp, vp, vp], C.c_int),
+        "pxg_adjoint_forward": ([vp, C.POINTER(RhsOp), vp, C.c_double, C.c_int, vp, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int), vp], C.c_int),
+        "pxg_adjoint_backward": ([vp, C.c_double, vp, vp, C.POINTER(C.c_int), vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -235,3 +242,27 @@ class Context:
 
     def interpolate(self, fn, coef, v, stream=None):
         self._check(self.L.pxg_interpolate(self.h, int(fn), float(coef), _ptr(v), stream), "interpolate")
+
+    # --- solve and adjoint
+    def cg(self, rp, ci, vals, b, x, rtol=1e-10, max_iter=10000, stream=None):
+        it, rel = C.c_int(), C.c_double()
+        self._check(self.L.pxg_cg(self.h, _ptr(rp), _ptr(ci), _ptr(vals), int(b.numel()), _ptr(b), _ptr(x),
+                                  float(rtol), int(max_iter), C.byref(it), C.byref(rel), stream), "cg")
+        return it.value, rel.value
+
+    def adjoint_grad(self, u, lam, g, stream=None):
+        self._check(self.L.pxg_adjoint_grad(self.h, _ptr(u), _ptr(lam), _ptr(g), stream), "adjoint_grad")
+
+    def adjoint_forward(self, rhs, u_target, rtol=1e-10, max_iter=20000, u_out=None, stream=None):
+        r = C.pointer(RhsOp(int(rhs.get("kind", 0)), int(rhs.get("fn", 0)), float(rhs.get("coef", 1.0)),
+                            _ptr(rhs.get("field")), 1))
+        loss, it = C.c_double(), C.c_int()
+        self._check(self.L.pxg_adjoint_forward(self.h, r, _ptr(u_target), float(rtol), int(max_iter), _ptr(u_out),
+                                               C.byref(loss), C.byref(it), stream), "adjoint_forward")
+        return loss.value, it.value
+
+    def adjoint_backward(self, grad, dloss=1.0, lam_out=None, stream=None):
+        it = C.c_int()
+        self._check(self.L.pxg_adjoint_backward(self.h, float(dloss), _ptr(grad), _ptr(lam_out), C.byref(it),
+                                                stream), "adjoint_backward")
+        return it.value

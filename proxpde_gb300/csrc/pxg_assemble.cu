@@ -646,6 +646,123 @@ __global__ void kCompact(int32_t const * __restrict__ rowPtr, int32_t const * __
     }
 }
 
+// Adjoint gradient g_e = -(C u)_e^T K_e (C lambda)_e for any element type (the
+// stiffness entries are those of kAssemble with the coefficient k_e).
+template <int T>
+__global__ void __launch_bounds__(128) kAdjointGrad(AdjArgs a)
+{
+  constexpr int NV = Elem<T>::NV, N = Elem<T>::N, NQ = Elem<T>::NQ;
+  constexpr bool HEX = Elem<T>::hex;
+  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.nelem)
+    return;
+  double X[NV][3];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    uint32_t const id = a.conn[e * NV + v];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      X[v][d] = a.xyz[3 * (int64_t)id + d];
+  }
+  double ue[N], le[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+  {
+    uint32_t const d = a.emap[e * N + i];
+    bool const c = a.bcMask && a.bcMask[d];
+    ue[i] = c ? 0. : a.u[d];
+    le[i] = c ? 0. : a.lam[d];
+  }
+  double G[HEX ? NQ : 1][6];
+  if constexpr (!HEX)
+  {
+    double J[3][3], A[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        J[r][cc] = X[cc + 1][r] - X[0][r];
+    double const det = adj3(J, A);
+    gram(A, 1.0 / fabs(det), G[0]);
+  }
+  else
+  {
+    double P[N][3];
+    mappingPoints<T>(X, P);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double J[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}}, A[3][3];
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc)
+            J[r][cc] += P[n][r] * DPHI<T>(q, n, cc);
+      double const det = adj3(J, A);
+      gram(A, WQ<T>(q) / fabs(det), G[q]);
+    }
+  }
+  double s = 0.;
+#pragma unroll 1
+  for (int i = 0; i < N; ++i)
+  {
+#pragma unroll 1
+    for (int j = i; j < N; ++j)
+    {
+      double kv = 0.;
+      if constexpr (HEX)
+      {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+        {
+          double const d0 = DPHI<T>(q, i, 0), d1 = DPHI<T>(q, i, 1), d2 = DPHI<T>(q, i, 2);
+          double const v0 = G[q][0] * d0 + G[q][3] * d1 + G[q][4] * d2;
+          double const v1 = G[q][3] * d0 + G[q][1] * d1 + G[q][5] * d2;
+          double const v2 = G[q][4] * d0 + G[q][5] * d1 + G[q][2] * d2;
+          kv += v0 * DPHI<T>(q, j, 0) + v1 * DPHI<T>(q, j, 1) + v2 * DPHI<T>(q, j, 2);
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+          kv += G[0][k] * TT<T>(k, i, j);
+      }
+      s += kv * ((i == j) ? ue[i] * le[i] : ue[i] * le[j] + ue[j] * le[i]);
+    }
+  }
+  a.g[e] = -(a.kE[e] * s);
+}
+
+pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, double * g, cudaStream_t s)
+{
+  AdjArgs a{c->nelem, c->xyz.p, c->conn.p, c->emap.p, c->kE.p, c->nbc ? c->bcMask.p : nullptr, u, lam, g};
+  unsigned const blocks = (unsigned)((c->nelem + 127) / 128);
+  switch (c->etype)
+  {
+  case P1TET:
+    kAdjointGrad<P1TET><<<blocks, 128, 0, s>>>(a);
+    break;
+  case P2TET:
+    kAdjointGrad<P2TET><<<blocks, 128, 0, s>>>(a);
+    break;
+  case Q1HEX:
+    if (c->q1Generic)
+      kAdjointGrad<Q1HEX><<<blocks, 128, 0, s>>>(a);
+    else
+      launchAdjointGradQ1(a, s);
+    break;
+  case Q2HEX:
+    kAdjointGrad<Q2HEX><<<blocks, 128, 0, s>>>(a);
+    break;
+  }
+  PXG_CUDA(c, cudaGetLastError());
+  return PXG_OK;
+}
+
 } // namespace pxg
 
 using namespace pxg;

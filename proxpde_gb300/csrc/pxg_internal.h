@@ -176,6 +176,34 @@ struct DevBuf
 
 } // namespace pxg
 
+// CG work vectors, device scalars and the internal stream used for graph capture
+struct CgWork
+{
+  int64_t n = 0;
+  pxg::DevBuf<double> r, z, p, q, dinv, part, scal;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t evIn = nullptr, evOut = nullptr;
+  ~CgWork()
+  {
+    if (stream)
+      cudaStreamDestroy(stream);
+    if (evIn)
+      cudaEventDestroy(evIn);
+    if (evOut)
+      cudaEventDestroy(evOut);
+  }
+};
+
+// state kept by pxg_adjoint_forward for pxg_adjoint_backward (the saved tensors)
+struct AdjState
+{
+  int64_t n = 0, nnz = 0;
+  pxg::DevBuf<double> K, M, b, u, w, Mw, lam, part;
+  double rtol = 1e-10;
+  int maxIter = 0;
+  bool valid = false;
+};
+
 // ----------------------------------------------------------------- context
 struct pxg_ctx
 {
@@ -207,6 +235,8 @@ struct pxg_ctx
   pxg::DevBuf<unsigned long long> counter;
   // PXG_Q1_GENERIC=1 in the environment selects the generic kernel for Q1 hexahedra
   bool q1Generic = false;
+  CgWork cg;
+  AdjState adj;
 };
 
 // arguments of the element kernels
@@ -239,6 +269,20 @@ struct AsmArgs
 };
 
 void launchAssembleQ1(AsmArgs const & a, cudaStream_t s);
+
+struct AdjArgs
+{
+  int64_t nelem;
+  double const * xyz;
+  uint32_t const * conn;
+  uint32_t const * emap;
+  double const * kE;
+  uint8_t const * bcMask;
+  double const * u;
+  double const * lam;
+  double * g;
+};
+void launchAdjointGradQ1(AdjArgs const & a, cudaStream_t s);
 } // namespace pxg
 
 // status helpers shared by the translation units
@@ -254,6 +298,12 @@ pxg_status buildPattern(pxg_ctx * c);
 
 // reference tables (pxg_assemble.cu)
 pxg_status initTables(pxg_ctx * c);
+// g_e = -(C u)_e^T K_e (C lambda)_e for every element (pxg_assemble.cu)
+pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, double * g, cudaStream_t s);
+// Jacobi-PCG (pxg_solve.cu)
+pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double const * a, int64_t n,
+                   double const * b, double * x, double rtol, int maxIter, int * itersOut, double * relOut,
+                   cudaStream_t user);
 } // namespace pxg
 
 #define PXG_CUDA(ctx, call)                                                                    \

@@ -72,44 +72,18 @@ __device__ __forceinline__ double sinpiNear(double so, double co, double o, doub
   }
   return sinpi(o + d);
 }
-} // namespace q1
 
-__global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
+// Per-element geometry at the 8 Gauss points: G[0..5][q] = xx yy zz xy xz yz entries
+// of adj(J) adj(J)^T / (4 |det J|), ad[q] = |det J_q|, off[q] = J_q xi_q.
+struct Q1Geo
 {
-  using namespace q1;
-  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= a.nelem)
-    return;
+  double G[6][8];
+  double ad[8];
+  double off[8][3];
+};
 
-  // ---- inputs: vertex ids, coordinates, DOF ids, BC flags
-  double X[8][3];
-  uint32_t dof[8];
-  {
-    uint4 const c0 = reinterpret_cast<uint4 const *>(a.conn)[2 * e];
-    uint4 const c1 = reinterpret_cast<uint4 const *>(a.conn)[2 * e + 1];
-    uint32_t const v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-#pragma unroll
-    for (int n = 0; n < 8; ++n)
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
-        X[n][d] = a.xyz[3 * (int64_t)v[n] + d];
-    uint4 const d0 = reinterpret_cast<uint4 const *>(a.emap)[2 * e];
-    uint4 const d1 = reinterpret_cast<uint4 const *>(a.emap)[2 * e + 1];
-    dof[0] = d0.x, dof[1] = d0.y, dof[2] = d0.z, dof[3] = d0.w;
-    dof[4] = d1.x, dof[5] = d1.y, dof[6] = d1.z, dof[7] = d1.w;
-  }
-  uint32_t cons = 0;
-  if (a.bcMask)
-  {
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      if (a.bcMask[dof[i]])
-        cons |= 1u << i;
-  }
-  double const kfac = a.kE ? a.kE[e] : 1.0;
-  bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
-  bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
-
+__device__ __forceinline__ void q1Geometry(double const (&X)[8][3], Q1Geo & geo)
+{
   // ---- Jacobian columns: Jc[axis][p][t][r] with p, t the quadrature coordinates of
   // the two other axes in increasing order and r the physical coordinate; column
   // `axis` of J is the bilinear interpolation of half the edge differences along it
@@ -145,8 +119,6 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
   }
 
   // ---- per quadrature point: adjugate, |det|, geometric factors
-  double Gxx[8], Gyy[8], Gzz[8], Gxy[8], Gxz[8], Gyz[8], ad[8];
-  double off[8][3]; // J_q xi_q (CurFE::qpoint minus origin)
 #pragma unroll
   for (int q = 0; q < 8; ++q)
   {
@@ -171,27 +143,29 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
     C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
     double const det = J[0][0] * C[0][0] + J[0][1] * C[1][0] + J[0][2] * C[2][0];
     double const adet = fabs(det);
-    ad[q] = adet;
+    geo.ad[q] = adet;
     double const s = 0.25 / adet;
-    Gxx[q] = s * (C[0][0] * C[0][0] + C[0][1] * C[0][1] + C[0][2] * C[0][2]);
-    Gyy[q] = s * (C[1][0] * C[1][0] + C[1][1] * C[1][1] + C[1][2] * C[1][2]);
-    Gzz[q] = s * (C[2][0] * C[2][0] + C[2][1] * C[2][1] + C[2][2] * C[2][2]);
-    Gxy[q] = s * (C[0][0] * C[1][0] + C[0][1] * C[1][1] + C[0][2] * C[1][2]);
-    Gxz[q] = s * (C[0][0] * C[2][0] + C[0][1] * C[2][1] + C[0][2] * C[2][2]);
-    Gyz[q] = s * (C[1][0] * C[2][0] + C[1][1] * C[2][1] + C[1][2] * C[2][2]);
+    geo.G[0][q] = s * (C[0][0] * C[0][0] + C[0][1] * C[0][1] + C[0][2] * C[0][2]);
+    geo.G[1][q] = s * (C[1][0] * C[1][0] + C[1][1] * C[1][1] + C[1][2] * C[1][2]);
+    geo.G[2][q] = s * (C[2][0] * C[2][0] + C[2][1] * C[2][1] + C[2][2] * C[2][2]);
+    geo.G[3][q] = s * (C[0][0] * C[1][0] + C[0][1] * C[1][1] + C[0][2] * C[1][2]);
+    geo.G[4][q] = s * (C[0][0] * C[2][0] + C[0][1] * C[2][1] + C[0][2] * C[2][2]);
+    geo.G[5][q] = s * (C[1][0] * C[2][0] + C[1][1] * C[2][1] + C[1][2] * C[2][2]);
     double const xq = qx ? g : -g, yq = qy ? g : -g, zq = qz ? g : -g;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
-      off[q][r] = J[r][0] * xq + J[r][1] * yq + J[r][2] * zq;
+      geo.off[q][r] = J[r][0] * xq + J[r][1] * yq + J[r][2] * zq;
   }
 
+}
+
+// Element stiffness with unit coefficient (upper triangle j >= i of Kl).
+__device__ __forceinline__ void q1Stiffness(Q1Geo const & geo, double (&Kl)[8][8])
+{
   // ---- stiffness (unit coefficient), upper triangle
-  double Kl[8][8];
-  if (needK)
   {
     // diagonal-direction tables S_a[c1][c2] (c1, c2 = classes of the two other axes)
     double S[3][3][3];
-    double const * Gd[3] = {Gxx, Gyy, Gzz};
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax)
     {
@@ -209,7 +183,7 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
             q0 = p + 4 * t, q1 = p + 2 + 4 * t;
           else
             q0 = p + 2 * t, q1 = p + 2 * t + 4;
-          H[p][t] = Gd[ax][q0] + Gd[ax][q1];
+          H[p][t] = geo.G[ax][q0] + geo.G[ax][q1];
         }
       double R[2][3];
 #pragma unroll
@@ -226,7 +200,6 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
     // cross tables, generic in the axis pair (a < b), third axis t:
     //   U_ab[first index][second index][class], entries sum_q G_ab l(qa) l(qb) W(qt)
     double U[3][2][2][3]; // pair 0 = xy, 1 = xz, 2 = yz
-    double const * Gc[3] = {Gxy, Gxz, Gyz};
 #pragma unroll
     for (int pr = 0; pr < 3; ++pr)
     {
@@ -244,7 +217,7 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
         for (int qb = 0; qb < 2; ++qb)
 #pragma unroll
           for (int c = 0; c < 3; ++c)
-            V[qa][qb][c] = cW(c, Gc[pr][qidx(qa, qb, 0)], Gc[pr][qidx(qa, qb, 1)]);
+            V[qa][qb][c] = cW(c, geo.G[3 + pr][qidx(qa, qb, 0)], geo.G[3 + pr][qidx(qa, qb, 1)]);
       double Y[2][2][3]; // [qa][b][c]
 #pragma unroll
       for (int qa = 0; qa < 2; ++qa)
@@ -283,6 +256,54 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
         Kl[i][j] = k;
       }
   }
+
+}
+
+} // namespace q1
+
+__global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
+{
+  using namespace q1;
+  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.nelem)
+    return;
+
+  // ---- inputs: vertex ids, coordinates, DOF ids, BC flags
+  double X[8][3];
+  uint32_t dof[8];
+  {
+    uint4 const c0 = reinterpret_cast<uint4 const *>(a.conn)[2 * e];
+    uint4 const c1 = reinterpret_cast<uint4 const *>(a.conn)[2 * e + 1];
+    uint32_t const v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        X[n][d] = a.xyz[3 * (int64_t)v[n] + d];
+    uint4 const d0 = reinterpret_cast<uint4 const *>(a.emap)[2 * e];
+    uint4 const d1 = reinterpret_cast<uint4 const *>(a.emap)[2 * e + 1];
+    dof[0] = d0.x, dof[1] = d0.y, dof[2] = d0.z, dof[3] = d0.w;
+    dof[4] = d1.x, dof[5] = d1.y, dof[6] = d1.z, dof[7] = d1.w;
+  }
+  uint32_t cons = 0;
+  if (a.bcMask)
+  {
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (a.bcMask[dof[i]])
+        cons |= 1u << i;
+  }
+  double const kfac = a.kE ? a.kE[e] : 1.0;
+  bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
+  bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
+
+  Q1Geo geo;
+  q1Geometry(X, geo);
+  double Kl[8][8];
+  if (needK)
+    q1Stiffness(geo, Kl);
+  double const (&ad)[8] = geo.ad;
+  double const (&off)[8][3] = geo.off;
 
   // ---- mass table Mt[cx][cy][cz] (unit coefficient)
   double Mt[3][3][3];
@@ -472,6 +493,53 @@ void launchAssembleQ1(AsmArgs const & a, cudaStream_t s)
 {
   unsigned const blocks = (unsigned)((a.nelem + 127) / 128);
   kAssembleQ1<<<blocks, 128, 0, s>>>(a);
+}
+
+// Adjoint gradient g_e = -(C u)_e^T K_e (C lambda)_e, K_e = k_e K0_e (Q1, 2x2x2 rule):
+// the same element stiffness as kAssembleQ1, contracted with the two local vectors.
+__global__ void __launch_bounds__(128) kAdjointGradQ1(AdjArgs a)
+{
+  using namespace q1;
+  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.nelem)
+    return;
+  double X[8][3], ue[8], le[8];
+  {
+    uint4 const c0 = reinterpret_cast<uint4 const *>(a.conn)[2 * e];
+    uint4 const c1 = reinterpret_cast<uint4 const *>(a.conn)[2 * e + 1];
+    uint32_t const v[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        X[n][d] = a.xyz[3 * (int64_t)v[n] + d];
+    uint4 const d0 = reinterpret_cast<uint4 const *>(a.emap)[2 * e];
+    uint4 const d1 = reinterpret_cast<uint4 const *>(a.emap)[2 * e + 1];
+    uint32_t const dof[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+    {
+      bool const c = a.bcMask && a.bcMask[dof[i]];
+      ue[i] = c ? 0. : a.u[dof[i]];
+      le[i] = c ? 0. : a.lam[dof[i]];
+    }
+  }
+  Q1Geo geo;
+  q1Geometry(X, geo);
+  double Kl[8][8];
+  q1Stiffness(geo, Kl);
+  double s = 0.;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = i; j < 8; ++j)
+      s = fma(Kl[i][j], (i == j) ? ue[i] * le[i] : fma(ue[i], le[j], ue[j] * le[i]), s);
+  a.g[e] = -(a.kE[e] * s);
+}
+
+void launchAdjointGradQ1(AdjArgs const & a, cudaStream_t s)
+{
+  kAdjointGradQ1<<<(unsigned)((a.nelem + 127) / 128), 128, 0, s>>>(a);
 }
 
 } // namespace pxg

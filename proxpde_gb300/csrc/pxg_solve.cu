@@ -1,0 +1,433 @@
+// Device Jacobi-preconditioned CG and the adjoint gradient of the diffusion loss
+//   K(k) u = b,   J(u) = 1/2 (u - u_t)^T M (u - u_t),   dJ/d log k_e = -(C u)_e^T K_e (C lambda)_e
+// with K lambda = M (u - u_t), K_e = k_e K0_e the element stiffness and C zeroing the
+// DOFs constrained by the essential BCs (the derivative of the condensed matrix
+// C K C + D is C K0_e C).  proxpde itself solves with UmfPackLU
+// (include/sparse_matrix.hpp:44); the CG here is plain and not an optimisation
+// target.
+//
+// CG design: every scalar (alpha, beta, r.z, residual, done flag, iteration count)
+// stays in device memory; dot products are reduced in two deterministic passes
+// (per-block partials, then one block); a chunk of iterations is captured once in a
+// CUDA graph and replayed, and the host reads the done flag once per chunk.  Kernels
+// after convergence return immediately, so a partly used chunk costs launches only.
+#include <cub/block/block_reduce.cuh>
+
+#include <cmath>
+#include <vector>
+
+#include "pxg_internal.h"
+
+namespace pxg
+{
+namespace
+{
+
+constexpr int kTpb = 256;
+constexpr int kMaxPartBlocks = 1024;
+constexpr int kChunk = 16; // CG iterations per captured graph
+
+enum : int
+{
+  S_RZ = 0,
+  S_PQ,
+  S_RZNEW,
+  S_RR,
+  S_BB,
+  S_ALPHA,
+  S_BETA,
+  S_DONE,
+  S_ITER,
+  S_TOL2,
+  S_MAXIT,
+  S_COUNT
+};
+
+inline int partBlocks(int64_t n)
+{
+  int64_t b = (n + kTpb - 1) / kTpb;
+  return (int)(b < kMaxPartBlocks ? b : kMaxPartBlocks);
+}
+
+template <int NV>
+__device__ __forceinline__ void blockSum(double (&v)[NV], double * out)
+{
+  using BR = cub::BlockReduce<double, kTpb>;
+  __shared__ typename BR::TempStorage ts;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+  {
+    double const s = BR(ts).Sum(v[k]);
+    if (threadIdx.x == 0)
+      out[k] = s;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kTpb) kDiagInv(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
+                                                 double const * __restrict__ a, int64_t n, double * __restrict__ dinv)
+{
+  int64_t const r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n)
+    return;
+  double d = 0.;
+  for (int32_t p = rp[r]; p < rp[r + 1]; ++p)
+    if (ci[p] == (int32_t)r)
+      d = a[p];
+  dinv[r] = (d != 0.) ? 1.0 / d : 1.0;
+}
+
+__global__ void __launch_bounds__(kTpb) kCgInit(double const * __restrict__ b, double const * __restrict__ dinv,
+                                                int64_t n, double * __restrict__ x, double * __restrict__ r,
+                                                double * __restrict__ z, double * __restrict__ p,
+                                                double * __restrict__ part)
+{
+  double acc[2] = {0., 0.};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    double const bi = b[i], zi = dinv[i] * bi;
+    x[i] = 0.;
+    r[i] = bi;
+    z[i] = zi;
+    p[i] = zi;
+    acc[0] += bi * zi;
+    acc[1] += bi * bi;
+  }
+  blockSum<2>(acc, part + 2 * blockIdx.x);
+}
+
+__global__ void kFinalInit(double const * __restrict__ part, int nb, double * __restrict__ s, double tol2,
+                           double maxit)
+{
+  if (threadIdx.x != 0)
+    return;
+  double rz = 0., bb = 0.;
+  for (int k = 0; k < nb; ++k)
+  {
+    rz += part[2 * k];
+    bb += part[2 * k + 1];
+  }
+  s[S_RZ] = rz;
+  s[S_BB] = bb;
+  s[S_RR] = bb;
+  s[S_ITER] = 0.;
+  s[S_TOL2] = tol2;
+  s[S_MAXIT] = maxit;
+  s[S_DONE] = (bb == 0.) ? 1. : 0.;
+}
+
+__global__ void __launch_bounds__(kTpb) kSpmvDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
+                                                 double const * __restrict__ a, double const * __restrict__ p,
+                                                 int64_t n, double * __restrict__ q, double * __restrict__ part,
+                                                 double const * __restrict__ s)
+{
+  if (s[S_DONE] != 0.)
+    return;
+  double acc[1] = {0.};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    double t = 0.;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+      t += a[k] * p[ci[k]];
+    q[i] = t;
+    acc[0] += p[i] * t;
+  }
+  blockSum<1>(acc, part + blockIdx.x);
+}
+
+__global__ void kFinalAlpha(double const * __restrict__ part, int nb, double * __restrict__ s)
+{
+  if (threadIdx.x != 0 || s[S_DONE] != 0.)
+    return;
+  double pq = 0.;
+  for (int k = 0; k < nb; ++k)
+    pq += part[k];
+  s[S_PQ] = pq;
+  s[S_ALPHA] = s[S_RZ] / pq;
+}
+
+__global__ void __launch_bounds__(kTpb) kCgUpdate(double * __restrict__ x, double * __restrict__ r,
+                                                  double const * __restrict__ p, double const * __restrict__ q,
+                                                  double const * __restrict__ dinv, double * __restrict__ z,
+                                                  int64_t n, double * __restrict__ part,
+                                                  double const * __restrict__ s)
+{
+  if (s[S_DONE] != 0.)
+    return;
+  double const al = s[S_ALPHA];
+  double acc[2] = {0., 0.};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    x[i] += al * p[i];
+    double const ri = r[i] - al * q[i];
+    r[i] = ri;
+    double const zi = dinv[i] * ri;
+    z[i] = zi;
+    acc[0] += ri * zi;
+    acc[1] += ri * ri;
+  }
+  blockSum<2>(acc, part + 2 * blockIdx.x);
+}
+
+__global__ void kFinalBeta(double const * __restrict__ part, int nb, double * __restrict__ s)
+{
+  if (threadIdx.x != 0 || s[S_DONE] != 0.)
+    return;
+  double rz = 0., rr = 0.;
+  for (int k = 0; k < nb; ++k)
+  {
+    rz += part[2 * k];
+    rr += part[2 * k + 1];
+  }
+  s[S_RR] = rr;
+  s[S_ITER] += 1.;
+  s[S_BETA] = rz / s[S_RZ];
+  s[S_RZ] = rz;
+  if (rr <= s[S_TOL2] * s[S_BB] || s[S_ITER] >= s[S_MAXIT] || !(rr == rr))
+    s[S_DONE] = 1.;
+}
+
+__global__ void __launch_bounds__(kTpb) kPUpdate(double * __restrict__ p, double const * __restrict__ z, int64_t n,
+                                                 double const * __restrict__ s)
+{
+  if (s[S_DONE] != 0.)
+    return;
+  double const be = s[S_BETA];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + be * p[i];
+}
+
+// y = A x and the dot x^T y (deterministic), for the loss
+__global__ void __launch_bounds__(kTpb) kSpmvPlainDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
+                                                      double const * __restrict__ a, double const * __restrict__ x,
+                                                      int64_t n, double * __restrict__ y, double * __restrict__ part)
+{
+  double acc[1] = {0.};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    double t = 0.;
+    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+      t += a[k] * x[ci[k]];
+    y[i] = t;
+    acc[0] += x[i] * t;
+  }
+  blockSum<1>(acc, part + blockIdx.x);
+}
+
+__global__ void kSub(double const * __restrict__ a, double const * __restrict__ b, int64_t n, double * __restrict__ c)
+{
+  int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n)
+    c[i] = a[i] - b[i];
+}
+
+__global__ void kScale(double * __restrict__ v, int64_t n, double s)
+{
+  int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n)
+    v[i] *= s;
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ CG driver
+pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double const * a, int64_t n,
+                   double const * b, double * x, double rtol, int maxIter, int * itersOut, double * relOut,
+                   cudaStream_t user)
+{
+  CgWork & w = c->cg;
+  if (w.n < n)
+  {
+    PXG_CUDA(c, w.r.alloc(n));
+    PXG_CUDA(c, w.z.alloc(n));
+    PXG_CUDA(c, w.p.alloc(n));
+    PXG_CUDA(c, w.q.alloc(n));
+    PXG_CUDA(c, w.dinv.alloc(n));
+    PXG_CUDA(c, w.part.alloc(2 * kMaxPartBlocks));
+    PXG_CUDA(c, w.scal.alloc(S_COUNT));
+    w.n = n;
+  }
+  if (!w.stream)
+    PXG_CUDA(c, cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
+  if (!w.evIn)
+  {
+    PXG_CUDA(c, cudaEventCreateWithFlags(&w.evIn, cudaEventDisableTiming));
+    PXG_CUDA(c, cudaEventCreateWithFlags(&w.evOut, cudaEventDisableTiming));
+  }
+  cudaStream_t const s = w.stream;
+  PXG_CUDA(c, cudaEventRecord(w.evIn, user));
+  PXG_CUDA(c, cudaStreamWaitEvent(s, w.evIn, 0));
+  int const nb = partBlocks(n);
+  unsigned const rows = (unsigned)((n + kTpb - 1) / kTpb);
+  kDiagInv<<<rows, kTpb, 0, s>>>(rp, ci, a, n, w.dinv.p);
+  kCgInit<<<nb, kTpb, 0, s>>>(b, w.dinv.p, n, x, w.r.p, w.z.p, w.p.p, w.part.p);
+  kFinalInit<<<1, 32, 0, s>>>(w.part.p, nb, w.scal.p, rtol * rtol, (double)maxIter);
+  PXG_CUDA(c, cudaGetLastError());
+
+  // capture one chunk of iterations
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  PXG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < kChunk; ++k)
+  {
+    kSpmvDot<<<nb, kTpb, 0, s>>>(rp, ci, a, w.p.p, n, w.q.p, w.part.p, w.scal.p);
+    kFinalAlpha<<<1, 32, 0, s>>>(w.part.p, nb, w.scal.p);
+    kCgUpdate<<<nb, kTpb, 0, s>>>(x, w.r.p, w.p.p, w.q.p, w.dinv.p, w.z.p, n, w.part.p, w.scal.p);
+    kFinalBeta<<<1, 32, 0, s>>>(w.part.p, nb, w.scal.p);
+    kPUpdate<<<nb, kTpb, 0, s>>>(w.p.p, w.z.p, n, w.scal.p);
+  }
+  cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (ce == cudaSuccess)
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph)
+    cudaGraphDestroy(graph);
+  if (ce != cudaSuccess)
+    return cudaFail(c, ce, "CG graph capture");
+  double h[S_COUNT];
+  pxg_status st = PXG_OK;
+  for (int launched = 0;; launched += kChunk)
+  {
+    ce = cudaGraphLaunch(exec, s);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(h, w.scal.p, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess)
+      ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess)
+    {
+      st = cudaFail(c, ce, "CG iterations");
+      break;
+    }
+    if (h[S_DONE] != 0. || launched + kChunk >= maxIter)
+      break;
+  }
+  cudaGraphExecDestroy(exec);
+  if (st != PXG_OK)
+    return st;
+  PXG_CUDA(c, cudaEventRecord(w.evOut, s));
+  PXG_CUDA(c, cudaStreamWaitEvent(user, w.evOut, 0));
+  double const rel = h[S_BB] > 0. ? std::sqrt(h[S_RR] / h[S_BB]) : 0.;
+  if (itersOut)
+    *itersOut = (int)h[S_ITER];
+  if (relOut)
+    *relOut = rel;
+  if (!(rel <= rtol))
+    return fail(c, PXG_ERR_NOT_CONVERGED, "CG stopped after %d iterations at relative residual %.3e (tol %.1e)",
+                (int)h[S_ITER], rel, rtol);
+  return PXG_OK;
+}
+
+} // namespace pxg
+
+using namespace pxg;
+
+extern "C"
+{
+
+pxg_status pxg_cg(pxg_ctx * c, int32_t const * row_ptr, int32_t const * col_idx, double const * vals, int64_t n,
+                  double const * b, double * x, double rtol, int max_iter, int * iters, double * rel_res,
+                  void * stream)
+{
+  if (!c || !row_ptr || !col_idx || !vals || !b || !x || n <= 0 || !(rtol > 0.) || max_iter <= 0)
+    return c ? fail(c, PXG_ERR_INVALID_ARG, "pxg_cg: bad argument") : PXG_ERR_INVALID_ARG;
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  return cgSolve(c, row_ptr, col_idx, vals, n, b, x, rtol, max_iter, iters, rel_res, (cudaStream_t)stream);
+}
+
+pxg_status pxg_adjoint_grad(pxg_ctx * c, double const * u, double const * lambda, double * g, void * stream)
+{
+  if (!c || !u || !lambda || !g)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->emap.p || !c->hasCoef)
+    return fail(c, PXG_ERR_INVALID_ARG, "adjoint gradient needs the DOF map and the coefficient");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  return launchAdjointGrad(c, u, lambda, g, (cudaStream_t)stream);
+}
+
+pxg_status pxg_adjoint_forward(pxg_ctx * c, pxg_rhs_op const * rhs, double const * u_target, double rtol,
+                               int max_iter, double * u_out, double * loss, int * iters, void * stream)
+{
+  if (!c || !rhs || !u_target || !loss)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->rowPtr.p || !c->hasCoef)
+    return fail(c, PXG_ERR_INVALID_ARG, "forward needs the pattern and the coefficient");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  AdjState & A = c->adj;
+  int64_t const n = c->ndof, nnz = c->nnz;
+  if (A.n != n || A.nnz != nnz)
+  {
+    PXG_CUDA(c, A.K.alloc(nnz));
+    PXG_CUDA(c, A.M.alloc(nnz));
+    PXG_CUDA(c, A.b.alloc(n));
+    PXG_CUDA(c, A.u.alloc(n));
+    PXG_CUDA(c, A.w.alloc(n));
+    PXG_CUDA(c, A.Mw.alloc(n));
+    PXG_CUDA(c, A.lam.alloc(n));
+    PXG_CUDA(c, A.part.alloc(kMaxPartBlocks));
+    A.n = n;
+    A.nnz = nnz;
+  }
+  A.valid = false;
+  // K(k) with BCs, M without, b = rhs with BCs (and the BC lift of K)
+  pxg_lhs_op const opK{2, 1.0, 0, 0.0, 1};
+  pxg_lhs_op const opM{0, 0.0, 1, 1.0, 0};
+  pxg_rhs_op r = *rhs;
+  r.apply_bc = 1;
+  if ((st = pxg_assemble(c, &opK, A.K.p, &opM, A.M.p, &r, A.b.p, 0u, stream)) != PXG_OK)
+    return st;
+  if ((st = cgSolve(c, c->rowPtr.p, c->colIdx.p, A.K.p, n, A.b.p, A.u.p, rtol, max_iter, iters, nullptr, s)) !=
+      PXG_OK)
+    return st;
+  unsigned const blocks = (unsigned)((n + kTpb - 1) / kTpb);
+  kSub<<<blocks, kTpb, 0, s>>>(A.u.p, u_target, n, A.w.p);
+  int const nb = partBlocks(n);
+  kSpmvPlainDot<<<nb, kTpb, 0, s>>>(c->rowPtr.p, c->colIdx.p, A.M.p, A.w.p, n, A.Mw.p, A.part.p);
+  PXG_CUDA(c, cudaGetLastError());
+  std::vector<double> hp(nb);
+  PXG_CUDA(c, cudaMemcpyAsync(hp.data(), A.part.p, nb * sizeof(double), cudaMemcpyDeviceToHost, s));
+  PXG_CUDA(c, cudaStreamSynchronize(s));
+  double J = 0.;
+  for (double v : hp)
+    J += v;
+  *loss = 0.5 * J;
+  if (u_out)
+    PXG_CUDA(c, cudaMemcpyAsync(u_out, A.u.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  A.rtol = rtol;
+  A.maxIter = max_iter;
+  A.valid = true;
+  return PXG_OK;
+}
+
+pxg_status pxg_adjoint_backward(pxg_ctx * c, double dloss, double * grad, double * lambda_out, int * iters,
+                                void * stream)
+{
+  if (!c || !grad)
+    return PXG_ERR_INVALID_ARG;
+  AdjState & A = c->adj;
+  if (!A.valid)
+    return fail(c, PXG_ERR_INVALID_ARG, "pxg_adjoint_backward needs a preceding pxg_adjoint_forward");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  // K lambda = M (u - u_t)  (K symmetric)
+  if ((st = cgSolve(c, c->rowPtr.p, c->colIdx.p, A.K.p, A.n, A.Mw.p, A.lam.p, A.rtol, A.maxIter, iters, nullptr,
+                    s)) != PXG_OK)
+    return st;
+  if ((st = launchAdjointGrad(c, A.u.p, A.lam.p, grad, s)) != PXG_OK)
+    return st;
+  if (dloss != 1.0)
+    kScale<<<(unsigned)((c->nelem + kTpb - 1) / kTpb), kTpb, 0, s>>>(grad, c->nelem, dloss);
+  if (lambda_out)
+    PXG_CUDA(c, cudaMemcpyAsync(lambda_out, A.lam.p, A.n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  PXG_CUDA(c, cudaGetLastError());
+  return PXG_OK;
+}
+
+} // extern "C"
