@@ -208,6 +208,28 @@ pxg_status pxg_adjoint_forward(pxg_ctx * ctx, const pxg_rhs_op * rhs, const doub
 pxg_status pxg_adjoint_backward(pxg_ctx * ctx, double dloss, double * grad, double * lambda_out,
                                 int * iters, void * stream);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent problems of one element type in one context: the mesh given to
+ * pxg_set_mesh is their disjoint union with the elements grouped by problem (problem
+ * p owns elements [elem_offsets[p], elem_offsets[p+1]), no node shared between
+ * problems).  First-touch numbering then gives each problem a contiguous DOF range.
+ * Call after pxg_build_pattern; elem_offsets is host memory (nprob + 1 values). */
+pxg_status pxg_batch_set(pxg_ctx * ctx, const int64_t * elem_offsets, int64_t nprob);
+/* For every problem of one or two batches (ctxs[0..nctx-1], same GPU): assemble
+ * K(k) with BCs, M and b (from `rhs`), solve K u = b, J_p = 1/2 (u-ut)^T M (u-ut),
+ * solve K lambda = M (u-ut), grad = dJ/dlog k_e.  The solves of all problems run in
+ * one persistent cooperative kernel with per-problem convergence (relative residual
+ * rtol); with use_graph the assembly, the solver and the gradient kernels are
+ * captured once in a CUDA graph and replayed while the arguments stay the same.
+ * u_targets[i]: device, ndof of ctxs[i]; grads[i]: device, nelem of ctxs[i];
+ * losses: host, one per problem (ctxs[0]'s problems first); iters: the largest CG
+ * iteration count.  PXG_ERR_TIMEOUT if a grid barrier wait of the persistent kernel
+ * ran out (the context stays usable). */
+pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, const pxg_rhs_op * rhs,
+                             const double * const * u_targets, double rtol, int max_iter,
+                             double * losses, double * const * grads, int * iters, int use_graph,
+                             void * stream);
+
 /* ----------------------------------------------------- allocation-free prune
  * No counterpart in proxpde: an allocation-free variant of pxg_close_matrix's
  * prune/compact for callers that cannot call cudaMalloc (code running where the

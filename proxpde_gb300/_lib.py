@@ -29,6 +29,7 @@ EXPORTS = [
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
     "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
+    "pxg_batch_set", "pxg_batch_adjoint",
 ]
 
 
@@ -98,6 +99,9 @@ def load(path: str = LIB_PATH):
         "pxg_adjoint_forward": ([vp, C.POINTER(RhsOp), vp, C.c_double, C.c_int, vp, C.POINTER(C.c_double),
                                  C.POINTER(C.c_int), vp], C.c_int),
         "pxg_adjoint_backward": ([vp, C.c_double, vp, vp, C.POINTER(C.c_int), vp], C.c_int),
+        "pxg_batch_set": ([vp, C.POINTER(C.c_int64), i64], C.c_int),
+        "pxg_batch_adjoint": ([C.POINTER(vp), C.c_int, C.POINTER(RhsOp), C.POINTER(vp), C.c_double, C.c_int,
+                               C.POINTER(C.c_double), C.POINTER(vp), C.POINTER(C.c_int), C.c_int, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "../../include/pxg.h"
 
@@ -204,6 +205,52 @@ struct AdjState
   bool valid = false;
 };
 
+// a context's mesh declared as a batch of independent problems (pxg_batch_set)
+struct BatchState
+{
+  bool ready = false;
+  int64_t nprob = 0;
+  int probBase = 0; // global id of this batch's first problem in the last solve
+  pxg::DevBuf<int64_t> elemOff, dofOff;
+  std::vector<int64_t> dofOffHost;
+  pxg::DevBuf<int32_t> rowProb;
+  pxg::DevBuf<double> K, M, b, u, lam, r, z, p, q, dinv, w, Mw;
+};
+
+// arguments a captured batch graph was built for
+struct GraphKey
+{
+  int nctx = 0;
+  void * ctx[2] = {nullptr, nullptr};
+  double const * ut[2] = {nullptr, nullptr};
+  double * grad[2] = {nullptr, nullptr};
+  pxg_rhs_op rhs{};
+  double rtol = 0.;
+  int maxIter = 0;
+  bool operator==(GraphKey const & o) const
+  {
+    return nctx == o.nctx && ctx[0] == o.ctx[0] && ctx[1] == o.ctx[1] && ut[0] == o.ut[0] && ut[1] == o.ut[1] &&
+           grad[0] == o.grad[0] && grad[1] == o.grad[1] && rhs.kind == o.rhs.kind && rhs.fn == o.rhs.fn &&
+           rhs.coef == o.rhs.coef && rhs.field == o.rhs.field && rtol == o.rtol && maxIter == o.maxIter;
+  }
+};
+
+// per-problem solver state of the persistent batch kernel (on the first context)
+struct BatchShared
+{
+  int nprob = 0;
+  pxg::DevBuf<double> acc;
+  pxg::DevBuf<int> done, itF, itA, err;
+  pxg::DevBuf<unsigned> bar;
+  cudaGraphExec_t exec = nullptr;
+  GraphKey key;
+  ~BatchShared()
+  {
+    if (exec)
+      cudaGraphExecDestroy(exec);
+  }
+};
+
 // ----------------------------------------------------------------- context
 struct pxg_ctx
 {
@@ -237,6 +284,8 @@ struct pxg_ctx
   bool q1Generic = false;
   CgWork cg;
   AdjState adj;
+  BatchState batch;
+  BatchShared bshared;
 };
 
 // arguments of the element kernels
