@@ -119,6 +119,86 @@ def cpu_sample(n_sample, threads):
     return conn.shape[0] / dt, dt
 
 
+def measure_adjoint(n=96, reps=2):
+    """Config 4: dJ/dlog k_e on the perturbed Q1 96^3 cube (Dirichlet on all faces,
+    f = 1, u_t = sin sin sin), device Jacobi-CG to 1e-10: forward + backward time."""
+    import torch
+
+    from proxpde_gb300.adjoint import DiffusionLoss, DiffusionProblem
+    from proxpde_gb300 import meshgen
+
+    P = DiffusionProblem.cube_q1(n, rtol=1e-10)
+    k = meshgen.lognormal(20261208, P.nelem, 1.0)
+    logk = torch.as_tensor(np.log(k)).cuda().requires_grad_(True)
+    DiffusionLoss.apply(logk, P).backward()  # warm-up
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        logk.grad = None
+        t0 = time.perf_counter()
+        DiffusionLoss.apply(logk, P).backward()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    t = min(ts)
+    return {"workload": f"q1hex perturbed {n}^3, K(k)u=1, Dirichlet all faces, J=1/2|u-u_t|_M^2",
+            "elements": P.nelem, "ndof": P.ndof, "grads_per_s": 1.0 / t, "ms_per_grad": 1e3 * t,
+            "cg_iters": {"forward": P.iters[0], "adjoint": P.iters[1]}, "rtol": 1e-10}
+
+
+def measure_batched(n_hex=128, n_tet=128, reps=3):
+    """Config 5: 256 ragged problems (n ~ U{8..48}); batched persistent graph vs the
+    same problems one at a time through the plain forward/backward pair."""
+    import torch
+
+    from proxpde_gb300 import batch
+    from proxpde_gb300.adjoint import DiffusionLoss, DiffusionProblem
+
+    probs = batch.make_problems(n_hex=n_hex, n_tet=n_tet)
+    groups = [batch.Batch([p for p in probs if p["etype"] == 2]), batch.Batch([p for p in probs if p["etype"] == 0])]
+    batch.batch_adjoint(groups)  # builds and replays the graph
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        losses, iters = batch.batch_adjoint(groups)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    tb = min(ts)
+    # sequential plain launches
+    plain = []
+    for p in probs:
+        P = DiffusionProblem(p["etype"], p["xyz"], p["conn"], bc_nodes=p["bc_nodes"], rtol=1e-10)
+        lk = torch.as_tensor(np.log(p["k"])).cuda().requires_grad_(True)
+        plain.append((P, lk))
+    def seq_pass():
+        out = []
+        for P, lk in plain:
+            lk.grad = None
+            DiffusionLoss.apply(lk, P).backward()
+            out.append(lk.grad)
+        torch.cuda.synchronize()
+        return out
+    seq_pass()
+    t0 = time.perf_counter()
+    gs = seq_pass()
+    ts_ = time.perf_counter() - t0
+    # batched vs plain gradients
+    err = 0.0
+    i = 0
+    for g in groups:
+        for q in range(g.nprob):
+            a, b = g.grad_of(q), gs[i]
+            err = max(err, float(torch.linalg.norm(a - b) / torch.linalg.norm(b)))
+            i += 1
+    E = sum(g.nelem for g in groups)
+    return {"workload": f"{n_hex} Q1-hex + {n_tet} P1-tet cubes, n~U{{8..48}}, K+M assembly + adjoint gradient",
+            "problems": n_hex + n_tet, "elements": E, "batched_grads_per_s": (n_hex + n_tet) / tb,
+            "sequential_grads_per_s": (n_hex + n_tet) / ts_, "speedup": ts_ / tb, "batched_ms": 1e3 * tb,
+            "sequential_ms": 1e3 * ts_, "max_cg_iters": iters,
+            "grad_rel_err_vs_plain": err, "rtol": 1e-10, "launch": "one CUDA graph: 2 assembly kernels, "
+            "1 persistent cooperative solver (forward CG, loss, adjoint CG), 2 gradient kernels"}
+
+
 def dist_init(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -168,6 +248,8 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-gradient measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
 
@@ -293,6 +375,12 @@ def main():
                "sample": f"{args.cpu_n}^3 Q1 hexes of the same workload (K+M+rhs), oracle restatement with OpenMP",
                "value_1thread": v_one, "sample_1thread": f"{min(args.cpu_n, 24)}^3 hexes, 1 thread"}
 
+    adjoint = batched = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = measure_adjoint()
+    if rank == 0 and not args.no_batched:
+        batched = measure_batched()
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -303,7 +391,7 @@ def main():
                        "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
                        "setup_s": setup_s, "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 3 * args.steps, "adjoint": adjoint, "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -134,41 +134,127 @@ __device__ __forceinline__ int sysOf(BatchDev const & d, int64_t g, int64_t & lr
   return 0;
 }
 
-// Warp-aggregated per-problem accumulation: lanes of a warp hold consecutive rows, so
-// they usually share a problem; then one atomic per warp and slot.
-template <int NV>
-__device__ __forceinline__ void accum(double * acc, int prob, double const (&v)[NV], int const (&slot)[NV])
+__device__ __forceinline__ int probOf(BatchDev const & d, int64_t g)
 {
-  unsigned const mask = __activemask();
-  int const p0 = __shfl_sync(mask, prob, __ffs(mask) - 1);
-  if (__all_sync(mask, prob == p0) && mask == 0xffffffffu)
+  int64_t lr;
+  int const sy = sysOf(d, g, lr);
+  return d.sys[sy].rowProb[lr];
+}
+
+// Per-block accumulation of per-problem sums.  Every block owns one contiguous range
+// of rows, so it meets a contiguous range of problem ids [pmin, pmin + nslot); each
+// lane keeps running sums while its problem does not change and flushes them into
+// shared-memory slots, and the block adds its slots into the global accumulators at
+// the end of the phase: one global atomic per block, problem and quantity.
+constexpr int kMaxSlot = 128;
+
+template <int NV>
+struct BlockAcc
+{
+  int pmin, nslot;
+  double v[kMaxSlot][NV];
+};
+
+template <int NV>
+__device__ __forceinline__ void baBegin(BlockAcc<NV> & ba, BatchDev const & d, int64_t r0, int64_t r1)
+{
+  __syncthreads(); // the previous phase's flush has finished reading the slots
+  if (threadIdx.x == 0)
   {
-#pragma unroll
-    for (int k = 0; k < NV; ++k)
+    if (r0 < r1)
     {
-      double s = v[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-        s += __shfl_xor_sync(mask, s, o);
-      if ((threadIdx.x & 31) == 0 && prob >= 0 && s != 0.)
-        atomicAdd(acc + (int64_t)prob * A_N + slot[k], s);
+      ba.pmin = probOf(d, r0);
+      ba.nslot = probOf(d, r1 - 1) - ba.pmin + 1;
+    }
+    else
+    {
+      ba.pmin = 0;
+      ba.nslot = 0;
     }
   }
-  else if (prob >= 0)
-  {
+  for (int k = threadIdx.x; k < kMaxSlot * NV; k += blockDim.x)
+    ba.v[k / NV][k % NV] = 0.;
+  __syncthreads();
+}
+
+template <int NV>
+struct LaneAcc
+{
+  int prob = -1;
+  double v[NV];
+};
+
+template <int NV>
+__device__ __forceinline__ void laFlush(LaneAcc<NV> & la, BlockAcc<NV> & ba, double * acc, int const (&slot)[NV])
+{
+  if (la.prob < 0)
+    return;
+  int const k = la.prob - ba.pmin;
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
-      if (v[k] != 0.)
-        atomicAdd(acc + (int64_t)prob * A_N + slot[k], v[k]);
+  for (int q = 0; q < NV; ++q)
+    if (la.v[q] != 0.)
+    {
+      if (k >= 0 && k < ba.nslot && k < kMaxSlot)
+        atomicAdd(&ba.v[k][q], la.v[q]);
+      else
+        atomicAdd(acc + (int64_t)la.prob * A_N + slot[q], la.v[q]);
+    }
+  la.prob = -1;
+}
+
+template <int NV>
+__device__ __forceinline__ void laAdd(LaneAcc<NV> & la, BlockAcc<NV> & ba, double * acc, int const (&slot)[NV],
+                                      int prob, double const (&v)[NV])
+{
+  if (prob != la.prob)
+  {
+    laFlush<NV>(la, ba, acc, slot);
+    la.prob = prob;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      la.v[q] = 0.;
   }
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    la.v[q] += v[q];
+}
+
+template <int NV>
+__device__ __forceinline__ void baEnd(BlockAcc<NV> & ba, LaneAcc<NV> & la, double * acc, int const (&slot)[NV])
+{
+  laFlush<NV>(la, ba, acc, slot);
+  __syncthreads();
+  int const n = ba.nslot < kMaxSlot ? ba.nslot : kMaxSlot;
+  for (int k = threadIdx.x; k < n * NV; k += blockDim.x)
+  {
+    double const x = ba.v[k / NV][k % NV];
+    if (x != 0.)
+      atomicAdd(acc + (int64_t)(ba.pmin + k / NV) * A_N + slot[k % NV], x);
+  }
+}
+
+// rows of this block
+__device__ __forceinline__ void blockRows(BatchDev const & d, int64_t & r0, int64_t & r1)
+{
+  int64_t const per = (d.total + gridDim.x - 1) / gridDim.x;
+  r0 = (int64_t)blockIdx.x * per;
+  if (r0 > d.total)
+    r0 = d.total;
+  r1 = r0 + per;
+  if (r1 > d.total)
+    r1 = d.total;
 }
 
 // One batched PCG solve: x = K^-1 rhs per problem.  `forward` selects (b -> u) or
 // (Mw -> lam).  Returns false on a barrier timeout.
-__device__ bool batchCg(BatchDev const & d, bool forward)
+__device__ bool batchCg(BatchDev const & d, bool forward, BlockAcc<2> & ba2, BlockAcc<1> & ba1)
 {
   int64_t const nthr = (int64_t)gridDim.x * blockDim.x;
   int64_t const tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t r0, r1;
+  blockRows(d, r0, r1);
+  constexpr int RPW = 32 / kLpr;
+  int const lane = threadIdx.x & 31, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
   // reset accumulators and flags
   for (int64_t k = tid; k < (int64_t)d.nprob * A_N; k += nthr)
     if ((k % A_N) != A_J)
@@ -180,18 +266,16 @@ __device__ bool batchCg(BatchDev const & d, bool forward)
   }
   if (!gridSync(d))
     return false;
-  // init: x = 0, r = rhs, z = D^-1 r, p = z; rz -> slot RZ1 (the "previous" parity of it = 0), bb
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < d.total; base += nthr)
+  // init: x = 0, r = rhs, z = D^-1 r, p = z; r.z into RZ1 (the slot iteration 0 reads), b.b
   {
-    int64_t const g = base + threadIdx.x;
-    int prob = -1;
-    double v[2] = {0., 0.};
-    if (g < d.total)
+    int const sl[2] = {A_RZ1, A_BB};
+    baBegin<2>(ba2, d, r0, r1);
+    LaneAcc<2> la;
+    for (int64_t g = r0 + threadIdx.x; g < r1; g += blockDim.x)
     {
       int64_t lr;
       SysDev const & s = d.sys[sysOf(d, g, lr)];
-      prob = s.rowProb[lr];
-      double const bi = forward ? s.b[lr] : s.Mw[lr];
+      double const bi = forward ? s.b[lr] : __ldcg(s.Mw + lr);
       double dd = 0.;
       for (int32_t k = s.rp[lr]; k < s.rp[lr + 1]; ++k)
         if (s.ci[k] == (int32_t)lr)
@@ -199,15 +283,14 @@ __device__ bool batchCg(BatchDev const & d, bool forward)
       double const di = dd != 0. ? 1.0 / dd : 1.0;
       s.dinv[lr] = di;
       double const zi = di * bi;
-      (forward ? s.u : s.lam)[lr] = 0.;
-      s.r[lr] = bi;
-      s.z[lr] = zi;
-      s.p[lr] = zi;
-      v[0] = bi * zi;
-      v[1] = bi * bi;
+      __stcg((forward ? s.u : s.lam) + lr, 0.);
+      __stcg(s.r + lr, bi);
+      __stcg(s.z + lr, zi);
+      __stcg(s.p + lr, zi);
+      double const v[2] = {bi * zi, bi * bi};
+      laAdd<2>(la, ba2, d.acc, sl, s.rowProb[lr], v);
     }
-    int const sl[2] = {A_RZ1, A_BB};
-    accum<2>(d.acc, prob, v, sl);
+    baEnd<2>(ba2, la, d.acc, sl);
   }
   if (!gridSync(d))
     return false;
@@ -227,82 +310,75 @@ __device__ bool batchCg(BatchDev const & d, bool forward)
         d.acc[(int64_t)k * A_N + A_RR0 + (par ^ 1)] = 0.;
         d.acc[(int64_t)k * A_N + A_RZ0 + par] = 0.;
       }
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < d.total; base += nthr)
     {
-      int64_t const g = base + threadIdx.x;
-      int prob = -1;
-      double v[1] = {0.};
-      if (g < d.total)
+      int const sl[1] = {A_PQ0 + par};
+      baBegin<1>(ba1, d, r0, r1);
+      LaneAcc<1> la;
+      for (int64_t g0 = r0 + (int64_t)warp * RPW; g0 < r1; g0 += (int64_t)nwarps * RPW)
       {
-        int64_t lr;
-        SysDev const & s = d.sys[sysOf(d, g, lr)];
-        int const pr = s.rowProb[lr];
-        if (!__ldcg(d.done + pr))
+        int64_t const g = g0 + lane / kLpr;
+        int64_t lr = 0;
+        int sy = 0, pr = -1;
+        bool act = false;
+        if (g < r1)
         {
-          prob = pr;
-          double t = 0.;
-          for (int32_t k = s.rp[lr]; k < s.rp[lr + 1]; ++k)
-            t += s.K[k] * __ldcg(s.p + s.ci[k]);
+          sy = sysOf(d, g, lr);
+          pr = d.sys[sy].rowProb[lr];
+          act = !__ldcg(d.done + pr);
+        }
+        SysDev const & s = d.sys[sy];
+        double const t = rowDot<true>(s.rp, s.ci, s.K, s.p, lr, act);
+        if (act && (lane & (kLpr - 1)) == 0)
+        {
           __stcg(s.q + lr, t);
-          v[0] = __ldcg(s.p + lr) * t;
+          double const v[1] = {__ldcg(s.p + lr) * t};
+          laAdd<1>(la, ba1, d.acc, sl, pr, v);
         }
       }
-      int const sl[1] = {A_PQ0 + par};
-      accum<1>(d.acc, prob, v, sl);
+      baEnd<1>(ba1, la, d.acc, sl);
     }
     if (!gridSync(d))
       return false;
     // S2: x += alpha p, r -= alpha q, z = D^-1 r ; r.z, r.r
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < d.total; base += nthr)
     {
-      int64_t const g = base + threadIdx.x;
-      int prob = -1;
-      double v[2] = {0., 0.};
-      if (g < d.total)
+      int const sl[2] = {A_RZ0 + par, A_RR0 + par};
+      baBegin<2>(ba2, d, r0, r1);
+      LaneAcc<2> la;
+      for (int64_t g = r0 + threadIdx.x; g < r1; g += blockDim.x)
       {
         int64_t lr;
         SysDev const & s = d.sys[sysOf(d, g, lr)];
         int const pr = s.rowProb[lr];
-        if (!__ldcg(d.done + pr))
-        {
-          prob = pr;
-          double const * a = d.acc + (int64_t)pr * A_N;
-          double const al = __ldcg(a + A_RZ0 + (par ^ 1)) / __ldcg(a + A_PQ0 + par);
-          double * x = forward ? s.u : s.lam;
-          double const pi = __ldcg(s.p + lr);
-          __stcg(x + lr, __ldcg(x + lr) + al * pi);
-          double const ri = __ldcg(s.r + lr) - al * __ldcg(s.q + lr);
-          __stcg(s.r + lr, ri);
-          double const zi = s.dinv[lr] * ri;
-          __stcg(s.z + lr, zi);
-          v[0] = ri * zi;
-          v[1] = ri * ri;
-        }
+        if (__ldcg(d.done + pr))
+          continue;
+        double const * a = d.acc + (int64_t)pr * A_N;
+        double const al = __ldcg(a + A_RZ0 + (par ^ 1)) / __ldcg(a + A_PQ0 + par);
+        double * x = forward ? s.u : s.lam;
+        __stcg(x + lr, __ldcg(x + lr) + al * __ldcg(s.p + lr));
+        double const ri = __ldcg(s.r + lr) - al * __ldcg(s.q + lr);
+        __stcg(s.r + lr, ri);
+        double const zi = s.dinv[lr] * ri;
+        __stcg(s.z + lr, zi);
+        double const v[2] = {ri * zi, ri * ri};
+        laAdd<2>(la, ba2, d.acc, sl, pr, v);
       }
-      int const sl[2] = {A_RZ0 + par, A_RR0 + par};
-      accum<2>(d.acc, prob, v, sl);
+      baEnd<2>(ba2, la, d.acc, sl);
     }
     if (!gridSync(d))
       return false;
     // S3: convergence per problem, p = z + beta p
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < d.total; base += nthr)
+    for (int64_t g = r0 + threadIdx.x; g < r1; g += blockDim.x)
     {
-      int64_t const g = base + threadIdx.x;
-      if (g < d.total)
+      int64_t lr;
+      SysDev const & s = d.sys[sysOf(d, g, lr)];
+      int const pr = s.rowProb[lr];
+      if (__ldcg(d.done + pr))
+        continue;
+      double const * a = d.acc + (int64_t)pr * A_N;
+      if (!(__ldcg(a + A_RR0 + par) <= d.tol2 * __ldcg(a + A_BB)))
       {
-        int64_t lr;
-        SysDev const & s = d.sys[sysOf(d, g, lr)];
-        int const pr = s.rowProb[lr];
-        if (!__ldcg(d.done + pr))
-        {
-          double const * a = d.acc + (int64_t)pr * A_N;
-          bool const conv = __ldcg(a + A_RR0 + par) <= d.tol2 * __ldcg(a + A_BB);
-          if (!conv)
-          {
-            double const be = __ldcg(a + A_RZ0 + par) / __ldcg(a + A_RZ0 + (par ^ 1));
-            __stcg(s.p + lr, __ldcg(s.z + lr) + be * __ldcg(s.p + lr));
-          }
-        }
+        double const be = __ldcg(a + A_RZ0 + par) / __ldcg(a + A_RZ0 + (par ^ 1));
+        __stcg(s.p + lr, __ldcg(s.z + lr) + be * __ldcg(s.p + lr));
       }
     }
     // bookkeeping by block 0 (other blocks only read `done` after the barrier)
@@ -336,44 +412,49 @@ __device__ bool batchCg(BatchDev const & d, bool forward)
 
 __global__ void __launch_bounds__(kBt) kBatchSolve(BatchDev d)
 {
-  if (!batchCg(d, true))
+  __shared__ BlockAcc<2> ba2;
+  __shared__ BlockAcc<1> ba1;
+  if (!batchCg(d, true, ba2, ba1))
     return;
   // loss: w = u - u_t, Mw = M w, J_p = 1/2 w.Mw
-  int64_t const nthr = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < d.total; base += nthr)
+  int64_t r0, r1;
+  blockRows(d, r0, r1);
+  for (int64_t g = r0 + threadIdx.x; g < r1; g += blockDim.x)
   {
-    int64_t const g = base + threadIdx.x;
-    if (g < d.total)
-    {
-      int64_t lr;
-      SysDev const & s = d.sys[sysOf(d, g, lr)];
-      __stcg(s.w + lr, __ldcg(s.u + lr) - s.ut[lr]);
-    }
+    int64_t lr;
+    SysDev const & s = d.sys[sysOf(d, g, lr)];
+    __stcg(s.w + lr, __ldcg(s.u + lr) - s.ut[lr]);
   }
   if (!gridSync(d))
     return;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < d.total; base += nthr)
   {
-    int64_t const g = base + threadIdx.x;
-    int prob = -1;
-    double v[1] = {0.};
-    if (g < d.total)
-    {
-      int64_t lr;
-      SysDev const & s = d.sys[sysOf(d, g, lr)];
-      prob = s.rowProb[lr];
-      double t = 0.;
-      for (int32_t k = s.rp[lr]; k < s.rp[lr + 1]; ++k)
-        t += s.M[k] * __ldcg(s.w + s.ci[k]);
-      __stcg(s.Mw + lr, t);
-      v[0] = 0.5 * __ldcg(s.w + lr) * t;
-    }
+    constexpr int RPW = 32 / kLpr;
+    int const lane = threadIdx.x & 31, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
     int const sl[1] = {A_J};
-    accum<1>(d.acc, prob, v, sl);
+    baBegin<1>(ba1, d, r0, r1);
+    LaneAcc<1> la;
+    for (int64_t g0 = r0 + (int64_t)warp * RPW; g0 < r1; g0 += (int64_t)nwarps * RPW)
+    {
+      int64_t const g = g0 + lane / kLpr;
+      int64_t lr = 0;
+      int sy = 0;
+      bool const valid = g < r1;
+      if (valid)
+        sy = sysOf(d, g, lr);
+      SysDev const & s = d.sys[sy];
+      double const t = rowDot<true>(s.rp, s.ci, s.M, s.w, lr, valid);
+      if (valid && (lane & (kLpr - 1)) == 0)
+      {
+        __stcg(s.Mw + lr, t);
+        double const v[1] = {0.5 * __ldcg(s.w + lr) * t};
+        laAdd<1>(la, ba1, d.acc, sl, s.rowProb[lr], v);
+      }
+    }
+    baEnd<1>(ba1, la, d.acc, sl);
   }
   if (!gridSync(d))
     return;
-  batchCg(d, false);
+  batchCg(d, false, ba2, ba1);
 }
 
 // DOF range of problem p: from the DOF of its first element's first slot (the first
@@ -527,7 +608,7 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
   PXG_CUDA(c0, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kBatchSolve, kBt, 0));
   if (perSm < 1)
     return fail(c0, PXG_ERR_CUDA, "persistent solver does not fit on an SM");
-  int const blocks = sms * (perSm < 2 ? perSm : 2);
+  int const blocks = sms * (perSm < 8 ? perSm : 8);
 
   cudaStream_t const s = (cudaStream_t)stream;
   auto record = [&](cudaStream_t rs) -> pxg_status {

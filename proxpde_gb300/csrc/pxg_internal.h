@@ -334,6 +334,51 @@ struct AdjArgs
 void launchAdjointGradQ1(AdjArgs const & a, cudaStream_t s);
 } // namespace pxg
 
+// Row-segment CSR product shared by the solvers: LPR consecutive lanes of a warp
+// work on one row (coalesced reads of the row's values and column ids), then reduce
+// with shuffles; every lane of the group returns the row's result.  All 32 lanes of
+// the warp must call it (valid = false for lanes without a row).
+namespace pxg
+{
+constexpr int kLpr = 4;  // lanes per row
+constexpr int kUnr = 8;  // entries per lane and load round
+template <bool L2ONLY>
+__device__ __forceinline__ double rowDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
+                                         double const * __restrict__ a, double const * x, int64_t row, bool valid)
+{
+  // kUnr strided entries per lane and round: their column ids and values are loaded
+  // together, then the gathers, so each lane keeps many loads in flight (a row of up
+  // to kLpr * kUnr = 32 entries takes one round)
+  int const sub = threadIdx.x & (kLpr - 1);
+  double t = 0.;
+  if (valid)
+  {
+    int32_t const e = rp[row + 1];
+    for (int32_t base = rp[row] + sub; base < e; base += kUnr * kLpr)
+    {
+      int32_t cc[kUnr];
+      double av[kUnr];
+#pragma unroll
+      for (int u = 0; u < kUnr; ++u)
+      {
+        int32_t const k = base + u * kLpr;
+        bool const ok = k < e;
+        cc[u] = ok ? ci[k] : -1;
+        av[u] = ok ? a[k] : 0.;
+      }
+#pragma unroll
+      for (int u = 0; u < kUnr; ++u)
+        if (cc[u] >= 0)
+          t = fma(av[u], L2ONLY ? __ldcg(x + cc[u]) : x[cc[u]], t);
+    }
+  }
+#pragma unroll
+  for (int o = kLpr / 2; o > 0; o >>= 1)
+    t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;
+}
+} // namespace pxg
+
 // status helpers shared by the translation units
 namespace pxg
 {

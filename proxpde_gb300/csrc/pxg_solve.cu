@@ -96,24 +96,39 @@ __global__ void __launch_bounds__(kTpb) kCgInit(double const * __restrict__ b, d
   blockSum<2>(acc, part + 2 * blockIdx.x);
 }
 
-__global__ void kFinalInit(double const * __restrict__ part, int nb, double * __restrict__ s, double tol2,
-                           double maxit)
+// Sum the per-block partials with one block (deterministic for a fixed grid).
+template <int NV>
+__device__ __forceinline__ void sumPartials(double const * __restrict__ part, int nb, double (&out)[NV])
 {
+  double v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+    v[k] = 0.;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      v[k] += part[NV * b + k];
+  __shared__ double res[NV];
+  blockSum<NV>(v, res);
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+    out[k] = res[k];
+}
+
+__global__ void __launch_bounds__(kTpb) kFinalInit(double const * __restrict__ part, int nb, double * __restrict__ s,
+                                                   double tol2, double maxit)
+{
+  double t[2];
+  sumPartials<2>(part, nb, t);
   if (threadIdx.x != 0)
     return;
-  double rz = 0., bb = 0.;
-  for (int k = 0; k < nb; ++k)
-  {
-    rz += part[2 * k];
-    bb += part[2 * k + 1];
-  }
-  s[S_RZ] = rz;
-  s[S_BB] = bb;
-  s[S_RR] = bb;
+  s[S_RZ] = t[0];
+  s[S_BB] = t[1];
+  s[S_RR] = t[1];
   s[S_ITER] = 0.;
   s[S_TOL2] = tol2;
   s[S_MAXIT] = maxit;
-  s[S_DONE] = (bb == 0.) ? 1. : 0.;
+  s[S_DONE] = (t[1] == 0.) ? 1. : 0.;
 }
 
 __global__ void __launch_bounds__(kTpb) kSpmvDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
@@ -124,26 +139,34 @@ __global__ void __launch_bounds__(kTpb) kSpmvDot(int32_t const * __restrict__ rp
   if (s[S_DONE] != 0.)
     return;
   double acc[1] = {0.};
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  constexpr int RPW = 32 / kLpr; // rows per warp step
+  int64_t const warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  int64_t const w = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  int const lane = threadIdx.x & 31;
+  for (int64_t r0 = w * RPW; r0 < n; r0 += warps * RPW)
   {
-    double t = 0.;
-    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
-      t += a[k] * p[ci[k]];
-    q[i] = t;
-    acc[0] += p[i] * t;
+    int64_t const row = r0 + lane / kLpr;
+    bool const valid = row < n;
+    double const t = rowDot<false>(rp, ci, a, p, row, valid);
+    if (valid && (lane & (kLpr - 1)) == 0)
+    {
+      q[row] = t;
+      acc[0] += p[row] * t;
+    }
   }
   blockSum<1>(acc, part + blockIdx.x);
 }
 
-__global__ void kFinalAlpha(double const * __restrict__ part, int nb, double * __restrict__ s)
+__global__ void __launch_bounds__(kTpb) kFinalAlpha(double const * __restrict__ part, int nb, double * __restrict__ s)
 {
-  if (threadIdx.x != 0 || s[S_DONE] != 0.)
+  if (s[S_DONE] != 0.)
     return;
-  double pq = 0.;
-  for (int k = 0; k < nb; ++k)
-    pq += part[k];
-  s[S_PQ] = pq;
-  s[S_ALPHA] = s[S_RZ] / pq;
+  double t[1];
+  sumPartials<1>(part, nb, t);
+  if (threadIdx.x != 0)
+    return;
+  s[S_PQ] = t[0];
+  s[S_ALPHA] = s[S_RZ] / t[0];
 }
 
 __global__ void __launch_bounds__(kTpb) kCgUpdate(double * __restrict__ x, double * __restrict__ r,
@@ -169,16 +192,15 @@ __global__ void __launch_bounds__(kTpb) kCgUpdate(double * __restrict__ x, doubl
   blockSum<2>(acc, part + 2 * blockIdx.x);
 }
 
-__global__ void kFinalBeta(double const * __restrict__ part, int nb, double * __restrict__ s)
+__global__ void __launch_bounds__(kTpb) kFinalBeta(double const * __restrict__ part, int nb, double * __restrict__ s)
 {
-  if (threadIdx.x != 0 || s[S_DONE] != 0.)
+  if (s[S_DONE] != 0.)
     return;
-  double rz = 0., rr = 0.;
-  for (int k = 0; k < nb; ++k)
-  {
-    rz += part[2 * k];
-    rr += part[2 * k + 1];
-  }
+  double t[2];
+  sumPartials<2>(part, nb, t);
+  if (threadIdx.x != 0)
+    return;
+  double const rz = t[0], rr = t[1];
   s[S_RR] = rr;
   s[S_ITER] += 1.;
   s[S_BETA] = rz / s[S_RZ];
@@ -203,13 +225,20 @@ __global__ void __launch_bounds__(kTpb) kSpmvPlainDot(int32_t const * __restrict
                                                       int64_t n, double * __restrict__ y, double * __restrict__ part)
 {
   double acc[1] = {0.};
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  constexpr int RPW = 32 / kLpr;
+  int64_t const warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  int64_t const w = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  int const lane = threadIdx.x & 31;
+  for (int64_t r0 = w * RPW; r0 < n; r0 += warps * RPW)
   {
-    double t = 0.;
-    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
-      t += a[k] * x[ci[k]];
-    y[i] = t;
-    acc[0] += x[i] * t;
+    int64_t const row = r0 + lane / kLpr;
+    bool const valid = row < n;
+    double const t = rowDot<false>(rp, ci, a, x, row, valid);
+    if (valid && (lane & (kLpr - 1)) == 0)
+    {
+      y[row] = t;
+      acc[0] += x[row] * t;
+    }
   }
   blockSum<1>(acc, part + blockIdx.x);
 }
@@ -261,7 +290,7 @@ pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double c
   unsigned const rows = (unsigned)((n + kTpb - 1) / kTpb);
   kDiagInv<<<rows, kTpb, 0, s>>>(rp, ci, a, n, w.dinv.p);
   kCgInit<<<nb, kTpb, 0, s>>>(b, w.dinv.p, n, x, w.r.p, w.z.p, w.p.p, w.part.p);
-  kFinalInit<<<1, 32, 0, s>>>(w.part.p, nb, w.scal.p, rtol * rtol, (double)maxIter);
+  kFinalInit<<<1, kTpb, 0, s>>>(w.part.p, nb, w.scal.p, rtol * rtol, (double)maxIter);
   PXG_CUDA(c, cudaGetLastError());
 
   // capture one chunk of iterations
@@ -271,9 +300,9 @@ pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double c
   for (int k = 0; k < kChunk; ++k)
   {
     kSpmvDot<<<nb, kTpb, 0, s>>>(rp, ci, a, w.p.p, n, w.q.p, w.part.p, w.scal.p);
-    kFinalAlpha<<<1, 32, 0, s>>>(w.part.p, nb, w.scal.p);
+    kFinalAlpha<<<1, kTpb, 0, s>>>(w.part.p, nb, w.scal.p);
     kCgUpdate<<<nb, kTpb, 0, s>>>(x, w.r.p, w.p.p, w.q.p, w.dinv.p, w.z.p, n, w.part.p, w.scal.p);
-    kFinalBeta<<<1, 32, 0, s>>>(w.part.p, nb, w.scal.p);
+    kFinalBeta<<<1, kTpb, 0, s>>>(w.part.p, nb, w.scal.p);
     kPUpdate<<<nb, kTpb, 0, s>>>(w.p.p, w.z.p, n, w.scal.p);
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
