@@ -67,7 +67,10 @@ typedef enum pxg_fn
   PXG_FN_CONST = 0,         /* f = c */
   PXG_FN_SIN3 = 1,          /* f = c sin(pi x) sin(pi y) sin(pi z) */
   PXG_FN_POISSON_RHS = 2,   /* f = c 2.5 pi^2 sin(pi x/2) sin(3 pi y/2)  (test/poisson3d*.cpp:27-33) */
-  PXG_FN_POISSON_EXACT = 3  /* f = c sin(pi x/2) sin(3 pi y/2)            (test/poisson3d*.cpp:35-40) */
+  PXG_FN_POISSON_EXACT = 3, /* f = c sin(pi x/2) sin(3 pi y/2)            (test/poisson3d*.cpp:35-40) */
+  PXG_FN_COORD_X = 4,       /* f = c x  (coordinates, e.g. to locate DOFs on a plane) */
+  PXG_FN_COORD_Y = 5,       /* f = c y */
+  PXG_FN_COORD_Z = 6        /* f = c z */
 } pxg_fn;
 
 typedef struct pxg_ctx pxg_ctx;
@@ -181,6 +184,14 @@ pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_pt
 /* Lagrange interpolation of an analytic function at the DOF points
  * (interpolateAnalyticFunction, include/fespace.hpp:195-271): v[ndof], device. */
 pxg_status pxg_interpolate(pxg_ctx * ctx, int fn, double coef, double * v, void * stream);
+
+/* ------------------------------------------------------------ device memory
+ * Device buffers on the context's GPU for callers that have no CUDA runtime of their
+ * own (the C++ Builder shim in include/proxgpu/builder.hpp uses them).  dir: 0 host
+ * to device, 1 device to host, 2 device to device; synchronous when stream is NULL. */
+pxg_status pxg_device_alloc(pxg_ctx * ctx, uint64_t bytes, void ** ptr);
+pxg_status pxg_device_free(pxg_ctx * ctx, void * ptr);
+pxg_status pxg_memcpy(pxg_ctx * ctx, void * dst, const void * src, uint64_t bytes, int dir, void * stream);
 
 /* ------------------------------------------------------- solve and adjoint
  * Jacobi-preconditioned CG on a device CSR matrix (symmetric positive definite):

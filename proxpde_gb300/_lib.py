@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "libpxg.so")
 P1TET, P2TET, Q1HEX, Q2HEX = 0, 1, 2, 3
 MEM_HOST, MEM_DEVICE = 0, 1
 FN_CONST, FN_SIN3, FN_POISSON_RHS, FN_POISSON_EXACT = 0, 1, 2, 3
+FN_COORD_X, FN_COORD_Y, FN_COORD_Z = 4, 5, 6
 ACCUMULATE = 1
 
 STATUS = {
@@ -29,7 +30,7 @@ EXPORTS = [
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
     "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
-    "pxg_batch_set", "pxg_batch_adjoint",
+    "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
 ]
 
 
@@ -100,6 +101,9 @@ def load(path: str = LIB_PATH):
                                  C.POINTER(C.c_int), vp], C.c_int),
         "pxg_adjoint_backward": ([vp, C.c_double, vp, vp, C.POINTER(C.c_int), vp], C.c_int),
         "pxg_batch_set": ([vp, C.POINTER(C.c_int64), i64], C.c_int),
+        "pxg_device_alloc": ([vp, C.c_uint64, C.POINTER(vp)], C.c_int),
+        "pxg_device_free": ([vp, vp], C.c_int),
+        "pxg_memcpy": ([vp, vp, vp, C.c_uint64, C.c_int, vp], C.c_int),
         "pxg_batch_adjoint": ([C.POINTER(vp), C.c_int, C.POINTER(RhsOp), C.POINTER(vp), C.c_double, C.c_int,
                                C.POINTER(C.c_double), C.POINTER(vp), C.POINTER(C.c_int), C.c_int, vp], C.c_int),
     }

@@ -402,4 +402,48 @@ pxg_status pxg_set_bc(pxg_ctx * c, uint32_t const * dofs, double const * vals, i
   return PXG_OK;
 }
 
+pxg_status pxg_device_alloc(pxg_ctx * c, uint64_t bytes, void ** ptr)
+{
+  if (!c || !ptr)
+    return PXG_ERR_INVALID_ARG;
+  *ptr = nullptr;
+  pxg_status s = ensureDevice(c);
+  if (s != PXG_OK)
+    return s;
+  if (bytes == 0)
+    return PXG_OK;
+  PXG_CUDA(c, cudaMalloc(ptr, bytes));
+  return PXG_OK;
+}
+
+pxg_status pxg_device_free(pxg_ctx * c, void * ptr)
+{
+  if (!c)
+    return PXG_ERR_INVALID_ARG;
+  pxg_status s = ensureDevice(c);
+  if (s != PXG_OK)
+    return s;
+  if (ptr)
+    PXG_CUDA(c, cudaFree(ptr));
+  return PXG_OK;
+}
+
+pxg_status pxg_memcpy(pxg_ctx * c, void * dst, void const * src, uint64_t bytes, int dir, void * stream)
+{
+  if (!c || (bytes && (!dst || !src)) || dir < 0 || dir > 2)
+    return c ? fail(c, PXG_ERR_INVALID_ARG, "pxg_memcpy: bad argument") : PXG_ERR_INVALID_ARG;
+  pxg_status s = ensureDevice(c);
+  if (s != PXG_OK)
+    return s;
+  if (bytes == 0)
+    return PXG_OK;
+  cudaMemcpyKind const k = dir == 0 ? cudaMemcpyHostToDevice : dir == 1 ? cudaMemcpyDeviceToHost
+                                                                        : cudaMemcpyDeviceToDevice;
+  if (stream)
+    PXG_CUDA(c, cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream));
+  else
+    PXG_CUDA(c, cudaMemcpy(dst, src, bytes, k));
+  return PXG_OK;
+}
+
 } // extern "C"

@@ -820,7 +820,7 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
   {
     if (rhs->kind < 0 || rhs->kind > 2)
       return fail(c, PXG_ERR_INVALID_ARG, "rhs kind %d", rhs->kind);
-    if (rhs->kind == 1 && (rhs->fn < 0 || rhs->fn > PXG_FN_POISSON_EXACT))
+    if (rhs->kind == 1 && (rhs->fn < 0 || rhs->fn > PXG_FN_COORD_Z))
       return fail(c, PXG_ERR_INVALID_ARG, "unknown analytic function %d", rhs->fn);
     if (rhs->kind == 2 && !rhs->field)
       return fail(c, PXG_ERR_INVALID_ARG, "projection needs a field");
@@ -926,7 +926,7 @@ pxg_status pxg_interpolate(pxg_ctx * c, int fn, double coef, double * v, void * 
     return PXG_ERR_INVALID_ARG;
   if (!c->emap.p)
     return fail(c, PXG_ERR_INVALID_ARG, "no DOF map");
-  if (fn < 0 || fn > PXG_FN_POISSON_EXACT)
+  if (fn < 0 || fn > PXG_FN_COORD_Z)
     return fail(c, PXG_ERR_INVALID_ARG, "unknown analytic function %d", fn);
   pxg_status st = ensureDevice(c);
   if (st != PXG_OK)

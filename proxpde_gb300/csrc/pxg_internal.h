@@ -129,6 +129,12 @@ __host__ __device__ inline double evalFn(int fn, double c, double x, double y, d
     return c * (2.5 * 3.141592653589793 * 3.141592653589793 * sinpi(0.5 * x) * sinpi(1.5 * y));
   case PXG_FN_POISSON_EXACT:
     return c * (sinpi(0.5 * x) * sinpi(1.5 * y));
+  case PXG_FN_COORD_X:
+    return c * x;
+  case PXG_FN_COORD_Y:
+    return c * y;
+  case PXG_FN_COORD_Z:
+    return c * z;
   }
   return __longlong_as_double(0x7ff8000000000000ll);
 #else
