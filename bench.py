@@ -43,6 +43,18 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def traffic_per_element():
+    """DRAM bytes per element of the assembly kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "kAssembleQ1_q1hex96.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_element:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def make_inputs(n, seed=20261205):
     from proxpde_gb300 import meshgen
 
@@ -334,8 +346,10 @@ def main():
     hbm, which = peaks()
     achieved = alg / (asm_ms * 1e-3) / 1e9
     # FP64 work of the kernel as written (flops per element)
+    tpe = traffic_per_element()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "peak_source": which, "kernel": "kAssemble<Q1HEX> (+memset of K, M, b)",
+            "traffic": tpe * E if tpe else None, "traffic_source": "ncu 96^3 capture scaled by elements",
+            "peak_source": which, "kernel": "kAssemble<Q1HEX> (+memset of K, M, b)",
             "kernel_ms": asm_ms, "algorithmic_bytes": alg}
 
     e2e = None
