@@ -753,7 +753,7 @@ pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, 
     if (c->q1Generic)
       kAdjointGrad<Q1HEX><<<blocks, 128, 0, s>>>(a);
     else
-      launchAdjointGradQ1(a, s);
+      launchAdjointGradQ1(a, s, c->q1Fp64);
     break;
   case Q2HEX:
     kAdjointGrad<Q2HEX><<<blocks, 128, 0, s>>>(a);
@@ -859,7 +859,7 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     if (c->q1Generic)
       launchAssemble<Q1HEX>(a, s);
     else
-      launchAssembleQ1(a, s);
+      launchAssembleQ1(a, s, c->q1Fp64);
     break;
   case Q2HEX:
     launchAssemble<Q2HEX>(a, s);

@@ -1,0 +1,151 @@
+// Double-float ("dfl") arithmetic on the FP32 pipe.
+//
+// GB300 runs FP64 at ~1/64 of its FP32 rate (ncu: FP32:FP64 = 64:1; measured 600 GFMA/s
+// FP64 vs 35 TFMA/s FP32).  A value is kept as an unevaluated sum h + l of two floats
+// (|l| <= ulp(h)), which carries ~48 significant bits.  The building blocks are the
+// classical error-free transformations, written here from their published definitions:
+//   - TwoSum (Knuth, TAOCP vol. 2, 4.2.2): s + e = a + b exactly, 6 flops;
+//   - FastTwoSum (Dekker 1971), valid for |a| >= |b|: 3 flops;
+//   - TwoProd with an FMA: p + e = a * b exactly, 2 flops;
+// combined into the double-word addition ("sloppy" variant) and multiplication of
+// Joldes, Muller and Popescu, "Tight and rigorous error bounds for basic building
+// blocks of double-word arithmetic", ACM TOMS 44(2), 2017 (algorithms 4 and 12).
+// Error: a product has relative error <= ~5 * 2^-48; a sum has absolute error
+// <= ~2^-47 (|a| + |b|), which is the normwise bound the assembled matrices need
+// (agreement with the FP64 reference to 1e-12 of the largest entry).
+//
+// The intrinsics __fadd_rn / __fmul_rn keep the compiler from contracting or
+// reordering the operations of the transformations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace pxg
+{
+
+// the dfl overloads below must not hide the double ones
+using ::fabs;
+using ::fma;
+
+struct dfl
+{
+  float h, l;
+};
+
+__device__ __forceinline__ dfl dflTwoSum(float a, float b)
+{
+  float const s = __fadd_rn(a, b);
+  float const bb = __fsub_rn(s, a);
+  float const e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+
+__device__ __forceinline__ dfl dflFastTwoSum(float a, float b)
+{
+  float const s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dfl operator+(dfl a, dfl b)
+{
+  dfl const s = dflTwoSum(a.h, b.h);
+  return dflFastTwoSum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dfl operator-(dfl a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b)
+{
+  float const p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return dflFastTwoSum(p, e);
+}
+__device__ __forceinline__ dfl & operator+=(dfl & a, dfl b) { return a = a + b; }
+__device__ __forceinline__ dfl & operator-=(dfl & a, dfl b) { return a = a - b; }
+__device__ __forceinline__ dfl fma(dfl a, dfl b, dfl c) { return a * b + c; }
+__device__ __forceinline__ dfl fabs(dfl a) { return a.h < 0.f ? -a : a; }
+__device__ __forceinline__ bool operator<(dfl a, float b) { return a.h < b; }
+
+// 1/a: float reciprocal refined by one Newton step in double-float
+__device__ __forceinline__ dfl rcp(dfl a)
+{
+  float const r0 = __frcp_rn(a.h);
+  dfl const one{1.f, 0.f};
+  dfl const e = one - a * dfl{r0, 0.f};
+  return dfl{r0, 0.f} + dfl{r0, 0.f} * e;
+}
+__device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
+
+// ---------------------------------------------------------------- conversions
+// Compile-time constants: split a double into its nearest float and the remainder.
+template <typename T>
+__host__ __device__ constexpr T cst(double x);
+template <>
+__host__ __device__ constexpr double cst<double>(double x)
+{
+  return x;
+}
+template <>
+__host__ __device__ constexpr dfl cst<dfl>(double x)
+{
+  return dfl{(float)x, (float)(x - (double)(float)x)};
+}
+
+// Run-time double -> dfl with integer operations only (the FP64 pipe, which also
+// executes F2F conversions on GB300, stays free): the high float takes the top 24
+// significant bits (truncated), the low float the remaining 29 bits times 2^(e-52).
+// Exact to 2^-47 relative for normal doubles of magnitude 2^-74 .. 2^127; values
+// outside that range (and zero) take the F2F path.
+__device__ __forceinline__ dfl toDfl(double x)
+{
+  unsigned long long const b = (unsigned long long)__double_as_longlong(x);
+  unsigned const hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  int const e = (int)((hi >> 20) & 0x7ffu);
+  if (e < 949 || e > 1150)
+  {
+    float const h = __double2float_rn(x);
+    return dfl{h, __double2float_rn(x - (double)h)};
+  }
+  unsigned const sign = hi & 0x80000000u;
+  float const h = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+  float const scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);
+  float l = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), scale);
+  return dfl{h, sign ? -l : l};
+}
+
+// float -> double by integer operations (exact; subnormal floats become zero)
+__device__ __forceinline__ double f2dExact(float f)
+{
+  unsigned const u = __float_as_uint(f);
+  unsigned const e = (u >> 23) & 0xffu;
+  if (e == 0u)
+    return 0.0;
+  if (e == 0xffu)
+    return (double)f;
+  unsigned long long const bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                  ((unsigned long long)(e + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// dfl -> double: exact conversions of both parts, one FP64 addition
+__device__ __forceinline__ double toDouble(dfl a) { return f2dExact(a.h) + f2dExact(a.l); }
+__device__ __forceinline__ double toDouble(double a) { return a; }
+
+template <typename T>
+__device__ __forceinline__ T fromDouble(double x);
+template <>
+__device__ __forceinline__ double fromDouble<double>(double x)
+{
+  return x;
+}
+template <>
+__device__ __forceinline__ dfl fromDouble<dfl>(double x)
+{
+  return toDfl(x);
+}
+
+} // namespace pxg

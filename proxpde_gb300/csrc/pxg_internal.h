@@ -286,8 +286,11 @@ struct pxg_ctx
   double bcDiag = 1.0;
   // small device scratch (counters, flags)
   pxg::DevBuf<unsigned long long> counter;
-  // PXG_Q1_GENERIC=1 in the environment selects the generic kernel for Q1 hexahedra
+  // Q1 hexahedra use the tensor-product kernel in double-float arithmetic; in the
+  // environment PXG_Q1_FP64=1 selects its FP64 variant and PXG_Q1_GENERIC=1 the
+  // generic kernel (both kept for cross-checks)
   bool q1Generic = false;
+  bool q1Fp64 = false;
   CgWork cg;
   AdjState adj;
   BatchState batch;
@@ -323,7 +326,7 @@ struct AsmArgs
   double * b;
 };
 
-void launchAssembleQ1(AsmArgs const & a, cudaStream_t s);
+void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64);
 
 struct AdjArgs
 {
@@ -337,7 +340,7 @@ struct AdjArgs
   double const * lam;
   double * g;
 };
-void launchAdjointGradQ1(AdjArgs const & a, cudaStream_t s);
+void launchAdjointGradQ1(AdjArgs const & a, cudaStream_t s, bool fp64);
 } // namespace pxg
 
 // Row-segment CSR product shared by the solvers: LPR consecutive lanes of a warp

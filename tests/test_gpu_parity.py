@@ -144,14 +144,17 @@ def test_invalid_inputs_rejected(engine):
     assert torch.isfinite(v).all()
 
 
-@pytest.mark.parametrize("generic", [False, True], ids=["q1-tensor-kernel", "q1-generic-kernel"])
+@pytest.mark.parametrize("kernel", ["dfl", "fp64", "generic"])
 @pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
-def test_q1_kernels_agree_with_oracle(engine, monkeypatch, generic, bc):
-    """Both Q1 kernels (the tensor-product one used by default and the generic one)
-    against the oracle: K(k_e) + M + sin3 load on a perturbed mesh, with and without
-    inhomogeneous Dirichlet data."""
-    monkeypatch.setenv("PXG_Q1_GENERIC", "1" if generic else "0")
-    n = 7
+@pytest.mark.parametrize("n", [7, 40])
+def test_q1_kernels_agree_with_oracle(engine, monkeypatch, kernel, bc, n):
+    """The three Q1 kernels against the oracle: the tensor-product kernel in
+    double-float arithmetic (default), its FP64 variant, and the generic kernel;
+    K(k_e) + M + sin3 load on a perturbed mesh, with and without inhomogeneous
+    Dirichlet data.  n = 40 takes the short-series path of the load (small offsets),
+    n = 7 the direct sinpi path."""
+    monkeypatch.setenv("PXG_Q1_GENERIC", "1" if kernel == "generic" else "0")
+    monkeypatch.setenv("PXG_Q1_FP64", "1" if kernel == "fp64" else "0")
     xyz, conn, k = problem("hex", n, 0.2, seed=21, sigma=1.0)
     em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
     bcarg, mask, val = None, None, None
