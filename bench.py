@@ -45,7 +45,7 @@ def peaks():
 
 def traffic_per_element():
     """DRAM bytes per element of the assembly kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "kAssembleQ1_q1hex96.md")
+    p = os.path.join(ROOT, "profiles", "kAssembleQ1Group_q1hex96.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_element:"):
@@ -132,7 +132,7 @@ def cpu_sample(n_sample, threads):
 
 
 def measure_adjoint(n=96, reps=2):
-    """Config 4: dJ/dlog k_e on the perturbed Q1 96^3 cube (Dirichlet on all faces,
+    """Adjoint gradient dJ/dlog k_e on the perturbed Q1 96^3 cube (Dirichlet on all faces,
     f = 1, u_t = sin sin sin), device Jacobi-CG to 1e-10: forward + backward time."""
     import torch
 
@@ -158,7 +158,7 @@ def measure_adjoint(n=96, reps=2):
 
 
 def measure_batched(n_hex=128, n_tet=128, reps=3):
-    """Config 5: 256 ragged problems (n ~ U{8..48}); batched persistent graph vs the
+    """Batched adjoint gradients of 256 ragged problems (n ~ U{8..48}); batched persistent graph vs the
     same problems one at a time through the plain forward/backward pair."""
     import torch
 
@@ -302,18 +302,20 @@ def main():
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
 
+    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+
     def step(i=None):
         if i is not None:
             ev[i][0].record(stream)
         ctx.assemble(op0=opK, vals0=K, op1=opM, vals1=M, rhs=rhs, b=b, stream=sp)
         if i is not None:
             ev[i][1].record(stream)
-        pk = ctx.prune_count(K, stream=sp)
-        pm = ctx.prune_count(M, stream=sp)
-        return pk, pm
+        # closeMatrix's prune check, stream-ordered (no host round trip inside a step)
+        ctx.prune_count_device(K, cnt[0:1], stream=sp)
+        ctx.prune_count_device(M, cnt[1:2], stream=sp)
 
     for _ in range(args.warmup):
-        pruned = step()
+        step()
     if world > 1:
         import torch.distributed as dist
 
@@ -325,9 +327,10 @@ def main():
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record(stream)
     for i in range(args.steps):
-        pruned = step(i)
+        step(i)
     stop.record(stream)
     torch.cuda.synchronize()
+    pruned = cnt.tolist()
     clocks = clk.stop()
     total_ms = start.elapsed_time(stop)
     if world > 1:
@@ -345,40 +348,66 @@ def main():
     alg = 4 * 8 * E + 4 * 8 * E + 8 * E + 24 * nn + 8 * nnz * 2 + 8 * ndof
     hbm, which = peaks()
     achieved = alg / (asm_ms * 1e-3) / 1e9
-    # FP64 work of the kernel as written (flops per element)
     tpe = traffic_per_element()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": tpe * E if tpe else None, "traffic_source": "ncu 96^3 capture scaled by elements",
-            "peak_source": which, "kernel": "kAssemble<Q1HEX> (+memset of K, M, b)",
+            "peak_source": which, "kernel": "kAssembleQ1Group (+memset of K, M, b)",
             "kernel_ms": asm_ms, "algorithmic_bytes": alg}
 
     e2e = None
     if not args.no_e2e:
-        # through the C ABI with host buffers: coordinates and coefficients uploaded
-        # from pinned memory each step, K, M, b read back into pinned memory
+        # through the C ABI with host buffers: every step uploads the coordinates and
+        # the coefficients from pinned memory and reads K, M, b and the two prune
+        # counts back into pinned memory.  Two output sets alternate, so that the
+        # read-back of step i (on a copy stream) overlaps the upload and the assembly
+        # of step i + 1.
         xyz_h = torch.from_numpy(xyz).pin_memory()
         k_h = torch.from_numpy(k).pin_memory()
-        K_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
-        M_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
-        b_h = torch.empty(ndof, dtype=torch.float64).pin_memory()
+        copy_stream = torch.cuda.Stream(dev)
+        sets = []
+        for j in range(2):
+            sets.append({
+                "K": K if j == 0 else torch.empty(nnz, dtype=torch.float64, device=dev),
+                "M": M if j == 0 else torch.empty(nnz, dtype=torch.float64, device=dev),
+                "b": b if j == 0 else torch.empty(ndof, dtype=torch.float64, device=dev),
+                "cnt": torch.zeros(2, dtype=torch.int64, device=dev),
+                "Kh": torch.empty(nnz, dtype=torch.float64).pin_memory(),
+                "Mh": torch.empty(nnz, dtype=torch.float64).pin_memory(),
+                "bh": torch.empty(ndof, dtype=torch.float64).pin_memory(),
+                "cnth": torch.full((2,), -1, dtype=torch.int64).pin_memory(),
+                "ready": torch.cuda.Event(), "done": torch.cuda.Event(), "used": False})
 
-        def e2e_step():
+        def e2e_step(i):
+            S = sets[i % 2]
+            if S["used"]:
+                stream.wait_event(S["done"])  # the set's previous read-back has finished
             ctx.set_coords(xyz_h, stream=sp)
             ctx.set_coef(k_h, stream=sp)
-            step()
-            K_h.copy_(K, non_blocking=True)
-            M_h.copy_(M, non_blocking=True)
-            b_h.copy_(b, non_blocking=True)
-            torch.cuda.synchronize()
+            ctx.assemble(op0=opK, vals0=S["K"], op1=opM, vals1=S["M"], rhs=rhs, b=S["b"], stream=sp)
+            ctx.prune_count_device(S["K"], S["cnt"][0:1], stream=sp)
+            ctx.prune_count_device(S["M"], S["cnt"][1:2], stream=sp)
+            S["ready"].record(stream)
+            copy_stream.wait_event(S["ready"])
+            with torch.cuda.stream(copy_stream):
+                S["Kh"].copy_(S["K"], non_blocking=True)
+                S["Mh"].copy_(S["M"], non_blocking=True)
+                S["bh"].copy_(S["b"], non_blocking=True)
+                S["cnth"].copy_(S["cnt"], non_blocking=True)
+            S["done"].record(copy_stream)
+            S["used"] = True
 
-        for _ in range(2):
-            e2e_step()
+        for i in range(2):
+            e2e_step(i)
+        torch.cuda.synchronize()
         t1 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
+        for i in range(args.steps):
+            e2e_step(i)
+        torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t1) / args.steps
+        assert all(S["cnth"].tolist() == pruned for S in sets), "prune counts differ between the two legs"
         e2e = {"value": world * E / e2e_s, "unit": UNIT, "h2d_bytes_per_step": xyz.nbytes + k.nbytes,
-               "d2h_bytes_per_step": 2 * nnz * 8 + ndof * 8, "ms_per_step": e2e_s * 1e3}
+               "d2h_bytes_per_step": 2 * nnz * 8 + ndof * 8 + 16, "ms_per_step": e2e_s * 1e3,
+               "overlap": "read-back of step i overlaps upload and assembly of step i + 1 (two output sets)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

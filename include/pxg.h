@@ -175,6 +175,10 @@ pxg_status pxg_assemble(pxg_ctx * ctx, const pxg_lhs_op * op0, double * vals0,
  * structural-pattern value array with |v| <= 1e-16.  0 means the structural pattern
  * and `vals` already are the closed matrix. */
 pxg_status pxg_prune_count(pxg_ctx * ctx, const double * vals, int64_t * pruned, void * stream);
+/* The same count, asynchronous: stream-ordered, it leaves the count in *pruned_dev
+ * (device memory, one int64) and returns without waiting, so that assembly, the check
+ * and the read-back of several steps can overlap. */
+pxg_status pxg_prune_count_device(pxg_ctx * ctx, const double * vals, int64_t * pruned_dev, void * stream);
 /* Compact: write the pruned CSR (row_ptr[ndof+1], col_idx, vals_out; device
  * pointers, capacity nnz) and its entry count. */
 pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_ptr,

@@ -28,7 +28,7 @@ EXPORTS = [
     "pxg_create", "pxg_destroy", "pxg_last_error", "pxg_status_string", "pxg_version",
     "pxg_set_mesh", "pxg_set_coords", "pxg_build_dofmap", "pxg_set_dofmap", "pxg_get_dofmap",
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
-    "pxg_assemble", "pxg_prune_count", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
+    "pxg_assemble", "pxg_prune_count", "pxg_prune_count_device", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
     "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
 ]
@@ -91,6 +91,7 @@ def load(path: str = LIB_PATH):
         "pxg_assemble": ([vp, C.POINTER(LhsOp), vp, C.POINTER(LhsOp), vp, C.POINTER(RhsOp), vp, C.c_uint, vp],
                          C.c_int),
         "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
+        "pxg_prune_count_device": ([vp, vp, vp, vp], C.c_int),
         "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_interpolate": ([vp, C.c_int, C.c_double, vp, vp], C.c_int),
         "pxg_prune_csr_noalloc": ([vp, vp, vp, i64, vp, vp, vp, i64p, vp], C.c_int),
@@ -241,6 +242,11 @@ class Context:
         n = C.c_int64()
         self._check(self.L.pxg_prune_count(self.h, _ptr(vals), C.byref(n), stream), "prune_count")
         return n.value
+
+    def prune_count_device(self, vals, out, stream=None):
+        """Asynchronous prune count into `out` (a one-element int64 device tensor)."""
+        assert str(out.dtype) == "torch.int64" and out.is_cuda and out.numel() >= 1
+        self._check(self.L.pxg_prune_count_device(self.h, _ptr(vals), _ptr(out), stream), "prune_count_device")
 
     def close_matrix(self, vals, rp, ci, vout, stream=None):
         n = C.c_int64()

@@ -859,7 +859,7 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     if (c->q1Generic)
       launchAssemble<Q1HEX>(a, s);
     else
-      launchAssembleQ1(a, s, c->q1Fp64);
+      launchAssembleQ1(a, s, c->q1Fp64, c->q1Thread);
     break;
   case Q2HEX:
     launchAssemble<Q2HEX>(a, s);
@@ -886,6 +886,23 @@ pxg_status pxg_prune_count(pxg_ctx * c, double const * vals, int64_t * pruned, v
   PXG_CUDA(c, cudaMemcpyAsync(&h, c->counter.p, 8, cudaMemcpyDeviceToHost, s));
   PXG_CUDA(c, cudaStreamSynchronize(s));
   *pruned = (int64_t)h;
+  return PXG_OK;
+}
+
+pxg_status pxg_prune_count_device(pxg_ctx * c, double const * vals, int64_t * pruned_dev, void * stream)
+{
+  if (!c || !vals || !pruned_dev)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->rowPtr.p)
+    return fail(c, PXG_ERR_INVALID_ARG, "no pattern built");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  auto * cnt = reinterpret_cast<unsigned long long *>(pruned_dev);
+  PXG_CUDA(c, cudaMemsetAsync(cnt, 0, 8, s));
+  kPruneCount<<<152 * 8, 256, 0, s>>>(vals, c->nnz, cnt);
+  PXG_CUDA(c, cudaGetLastError());
   return PXG_OK;
 }
 

@@ -29,7 +29,7 @@ namespace pxg
 using ::fabs;
 using ::fma;
 
-struct dfl
+struct __align__(8) dfl
 {
   float h, l;
 };
@@ -94,41 +94,44 @@ __host__ __device__ constexpr dfl cst<dfl>(double x)
   return dfl{(float)x, (float)(x - (double)(float)x)};
 }
 
+// Rare path of toDfl (magnitudes outside 2^-74 .. 2^127): kept out of line, so that
+// the compiler does not predicate its FP64-pipe conversions into every call.
+__device__ __noinline__ dfl toDflSlow(double x)
+{
+  float const h = __double2float_rn(x);
+  return dfl{h, __double2float_rn(x - (double)h)};
+}
+
 // Run-time double -> dfl with integer operations only (the FP64 pipe, which also
 // executes F2F conversions on GB300, stays free): the high float takes the top 24
 // significant bits (truncated), the low float the remaining 29 bits times 2^(e-52).
-// Exact to 2^-47 relative for normal doubles of magnitude 2^-74 .. 2^127; values
-// outside that range (and zero) take the F2F path.
+// Exact to 2^-47 relative for normal doubles of magnitude 2^-74 .. 2^127; zero and
+// subnormals give zero, other values outside that range take toDflSlow.
 __device__ __forceinline__ dfl toDfl(double x)
 {
   unsigned long long const b = (unsigned long long)__double_as_longlong(x);
   unsigned const hi = (unsigned)(b >> 32), lo = (unsigned)b;
   int const e = (int)((hi >> 20) & 0x7ffu);
-  if (e < 949 || e > 1150)
-  {
-    float const h = __double2float_rn(x);
-    return dfl{h, __double2float_rn(x - (double)h)};
-  }
+  if (e != 0 && (e < 949 || e > 1150))
+    return toDflSlow(x);
   unsigned const sign = hi & 0x80000000u;
   float const h = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
   float const scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);
-  float l = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), scale);
-  return dfl{h, sign ? -l : l};
+  float const l = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), scale);
+  return e == 0 ? dfl{0.f, 0.f} : dfl{h, sign ? -l : l};
 }
 
-// float -> double by integer operations (exact; subnormal floats become zero)
+// float -> double by integer operations, branch-free (exact; subnormal floats become
+// zero, infinities and NaNs keep their class)
 __device__ __forceinline__ double f2dExact(float f)
 {
   unsigned const u = __float_as_uint(f);
-  unsigned const e = (u >> 23) & 0xffu;
-  if (e == 0u)
-    return 0.0;
-  if (e == 0xffu)
-    return (double)f;
-  unsigned long long const bits = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                  ((unsigned long long)(e + 896u) << 52) |
-                                  ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
+  unsigned const a = u & 0x7fffffffu;
+  unsigned hi = (a >> 3) + 0x38000000u; // exponent rebased by 1023 - 127
+  hi = a >= 0x7f800000u ? ((a >> 3) | 0x7ff00000u) : hi;
+  hi = a < 0x00800000u ? 0u : hi;
+  unsigned const lo = a < 0x00800000u ? 0u : u << 29;
+  return __hiloint2double((int)(hi | (u & 0x80000000u)), (int)lo);
 }
 
 // dfl -> double: exact conversions of both parts, one FP64 addition

@@ -291,6 +291,7 @@ struct pxg_ctx
   // generic kernel (both kept for cross-checks)
   bool q1Generic = false;
   bool q1Fp64 = false;
+  bool q1Thread = false;
   CgWork cg;
   AdjState adj;
   BatchState batch;
@@ -326,7 +327,7 @@ struct AsmArgs
   double * b;
 };
 
-void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64);
+void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread);
 
 struct AdjArgs
 {

@@ -87,6 +87,11 @@ __device__ __forceinline__ void addSgn(T & k, int a, int b, T v)
     k = k - v;
 }
 
+// The direct paths of sinpiNear (offsets beyond the short series), out of line so
+// that their FP64 code is not predicated into every call.
+__device__ __noinline__ double sinpiFar(double o, double d) { return sinpi(o + d); }
+__device__ __noinline__ dfl sinpiFar(double o, dfl d) { return toDfl(sinpi(o + toDouble(d))); }
+
 // sin(pi x) near a point whose sincospi is known: x = o + d
 __device__ __forceinline__ double sinpiNear(double so, double co, double o, double d)
 {
@@ -99,7 +104,7 @@ __device__ __forceinline__ double sinpiNear(double so, double co, double o, doub
     double const c = fma(u2, fma(u2, fma(u2, fma(u2, 1.0 / 40320.0, -1.0 / 720.0), 1.0 / 24.0), -0.5), 1.0);
     return fma(so, c, co * s);
   }
-  return sinpi(o + d);
+  return sinpiFar(o, d);
 }
 // The same in double-float.  For |u| < 0.05 the terms u^4/120 (< 6e-8) and beyond,
 // and u^4/24 (< 3e-7) and beyond, are needed to 1e-14 absolute only, which float
@@ -118,7 +123,7 @@ __device__ __forceinline__ dfl sinpiNear(dfl so, dfl co, double o, dfl d)
     dfl const s = u + u * es;
     return so * c + co * s;
   }
-  return toDfl(sinpi(o + toDouble(d)));
+  return sinpiFar(o, d);
 }
 
 // Per-element geometry at the 8 Gauss points: G[0..5][q] = xx yy zz xy xz yz entries
@@ -549,13 +554,504 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
   }
 }
 
-void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64)
+// =====================================================================================
+// Eight lanes per element (the default Q1 kernel).
+//
+// With one thread per element, the dynamically indexed arrays of the tensor-product
+// formulation (about 2 KB a thread) live in local memory. At full occupancy that is
+// about 330 MB, beyond the 129 MB L2, and it streams through HBM (ncu: ~5 KB of DRAM
+// traffic per element against ~1 KB of algorithmic traffic). Here a group of eight
+// lanes takes one element and the element's shared state (1 KB) lives in shared
+// memory. Lane l stands for the vertex and the Gauss point at lattice position
+// (l & 1, (l >> 1) & 1, l >> 2); proxpde's number of that vertex is l ^ bit1(l).
+//  A. lane = Gauss point q: the Jacobian by 2-point transforms across the lanes
+//     (shuffles), then adj(J), |det J|, G_q and the offset J_q xi_q;
+//  D. the load vector: f at the Gauss point, then the transposed transforms give the
+//     node values;
+//  B. lane = table job: the eight contractions over q of the tensor-product
+//     formulation: S_x, S_y, S_z, U_xy, U_xz, U_yz and the mass tables Sa, Sb with
+//     Mt[cx][cy][cz] = alpha_cx Sa[cy][cz] + beta_cx Sb[cy][cz], where
+//     W_c(q) = alpha_c + beta_c (-1)^q; one code path with per-lane weights;
+//  C. lane = matrix entries: the 36 pairs i <= j dealt round-robin; an entry is a
+//     signed sum of nine table values (two more for the mass), scaled per operator
+//     and scattered with FP64 reductions.
+namespace q1g
 {
-  unsigned const blocks = (unsigned)((a.nelem + 127) / 128);
+using namespace q1;
+
+// Threads per block.  The phases end at block barriers: the eight warps of a block
+// then run the same phase, and the SM's instruction cache holds the code of at most
+// four phases (one per resident block).  Measured at 128^3 (ms per launch): 128
+// threads with warp-level syncs 3.11, 128 / 256 / 512 / 1024 threads with block
+// barriers 3.03 / 2.77 / 3.09 / 3.40; 256 threads at 80 registers 2.99.
+constexpr int kThreads = 256;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr double kAlpha01 = 0.5 * (AA + BB), kBeta0 = 0.5 * (AA - BB);
+
+template <typename T>
+struct __align__(16) ElemShared
+{
+  union
+  {
+    T G[7][8];     // A -> B: G_xx, G_yy, G_zz, G_xy, G_xz, G_yz and |det J| per Gauss point
+    T tab[8 * 12]; // B -> C: tables, [job * 12 + row * 3 + class]
+  } u;
+  double bv[8];      // Dirichlet value of each node (0 when free)
+  int32_t rp[8];     // rowPtr of each node's DOF
+  uint32_t dof[8];
+  uint16_t rank[64]; // scatter ranks of the element's 8 x 8 entries
+  uint32_t pad[16];  // slot stride 1088 B: the four groups of a warp start 16 banks apart
+};
+constexpr size_t kSmemBytes = (kThreads / 8) * sizeof(ElemShared<dfl>) + 36 * sizeof(uint4);
+
+__device__ __forceinline__ dfl shx(dfl v, int m)
+{
+  return dfl{__shfl_xor_sync(kFull, v.h, m), __shfl_xor_sync(kFull, v.l, m)};
+}
+__device__ __forceinline__ double shx(double v, int m) { return __shfl_xor_sync(kFull, v, m); }
+__device__ __forceinline__ dfl shs(dfl v, int src)
+{
+  return dfl{__shfl_sync(kFull, v.h, src), __shfl_sync(kFull, v.l, src)};
+}
+__device__ __forceinline__ double shs(double v, int src) { return __shfl_sync(kFull, v, src); }
+// v * (bit ? 1/2 : -1/2)
+__device__ __forceinline__ dfl halfSgn(dfl v, int bit)
+{
+  float const s = bit ? 0.5f : -0.5f;
+  return dfl{v.h * s, v.l * s};
+}
+__device__ __forceinline__ double halfSgn(double v, int bit) { return v * (bit ? 0.5 : -0.5); }
+// n ? -v : v, n in {0, 1}
+__device__ __forceinline__ dfl negIf(dfl v, uint32_t n)
+{
+  uint32_t const m = n << 31;
+  return dfl{__uint_as_float(__float_as_uint(v.h) ^ m), __uint_as_float(__float_as_uint(v.l) ^ m)};
+}
+__device__ __forceinline__ double negIf(double v, uint32_t n) { return n ? -v : v; }
+__device__ __forceinline__ dfl scl(dfl v, float s) { return dfl{v.h * s, v.l * s}; }
+__device__ __forceinline__ double scl(double v, double s) { return v * s; }
+// 2-point transform along the axis of lane mask m: at the lane with bit b,
+// sum_n L(n, b) v(n) = A v(b) + B v(1 - b) (node values -> Gauss point, and back)
+template <typename T>
+__device__ __forceinline__ T lerp2(T v, int m)
+{
+  return cst<T>(A) * v + cst<T>(B) * shx(v, m);
+}
+
+// sin(pi o), cos(pi o): o = k/2 + r with |r| <= 1/4 (exact in FP64; adding 1.5 * 2^52
+// rounds 2o to an integer), Taylor polynomials of sin and cos at x = pi r with the
+// terms above 2^-24 in double-float and the rest in float, then the quadrant k mod 4.
+__device__ __forceinline__ void sinCosPiG(double o, dfl & s, dfl & c)
+{
+  constexpr double kRound = 6755399441055744.0;
+  double const kk = fma(2.0, o, kRound);
+  int const quad = __double2loint(kk) & 3;
+  double const r = fma(-0.5, kk - kRound, o);
+  dfl const x = toDfl(r) * cst<dfl>(PI);
+  dfl const t = x * x;
+  float const tf = t.h;
+  // sin x / x = 1 - t/3! + t^2/5! - t^3/7! + t^4/9! - t^5/11! + t^6/13! - t^7/15!
+  float const ps = tf * (-1.f / 39916800.f + tf * (1.f / 6227020800.f - tf * (1.f / 1307674368000.f)));
+  dfl hs = cst<dfl>(1.0 / 362880.0) + dfl{ps, 0.f};
+  hs = cst<dfl>(-1.0 / 5040.0) + t * hs;
+  hs = cst<dfl>(1.0 / 120.0) + t * hs;
+  hs = cst<dfl>(-1.0 / 6.0) + t * hs;
+  hs = cst<dfl>(1.0) + t * hs;
+  dfl const sr = x * hs;
+  // cos x = 1 - t/2! + t^2/4! - t^3/6! + t^4/8! - t^5/10! + t^6/12! - t^7/14! + t^8/16!
+  float const pc =
+      tf * (-1.f / 3628800.f + tf * (1.f / 479001600.f + tf * (-1.f / 87178291200.f + tf * (1.f / 20922789888000.f))));
+  dfl hc = cst<dfl>(1.0 / 40320.0) + dfl{pc, 0.f};
+  hc = cst<dfl>(-1.0 / 720.0) + t * hc;
+  hc = cst<dfl>(1.0 / 24.0) + t * hc;
+  hc = cst<dfl>(-0.5) + t * hc;
+  hc = cst<dfl>(1.0) + t * hc;
+  dfl const sa = (quad & 1) ? hc : sr, ca = (quad & 1) ? sr : hc;
+  s = negIf(sa, (quad >> 1) & 1);
+  c = negIf(ca, ((quad + 1) >> 1) & 1);
+}
+__device__ __forceinline__ void sinCosPiG(double o, double & s, double & c) { sincospi(o, &s, &c); }
+
+// Job t of phase B: G component, strides of the axes (u, v, w) in the Gauss point index
+// (as log2), kind (0 = sum along u, 1 = alternating sum along u, 2 = l_a along u and v).
+//   0 S_x: G_xx (x, y, z)   1 S_y: G_yy (y, x, z)   2 S_z: G_zz (z, x, y)
+//   3 Sa: |det J| (x, y, z) 4 Sb: |det J| (x, y, z) 5 U_xy: G_xy (x, y, z)
+//   6 U_xz: G_xz (x, z, y)  7 U_yz: G_yz (y, z, x)
+constexpr uint64_t jobc(uint64_t cmp, uint64_t su, uint64_t sv, uint64_t sw, uint64_t kind)
+{
+  return cmp | su << 3 | sv << 5 | sw << 7 | kind << 9;
+}
+constexpr uint64_t kJobsLo = jobc(0, 0, 1, 2, 0) | jobc(1, 1, 0, 2, 0) << 16 | jobc(2, 2, 0, 1, 0) << 32 |
+                             jobc(6, 0, 1, 2, 0) << 48;
+constexpr uint64_t kJobsHi = jobc(6, 0, 1, 2, 1) | jobc(3, 0, 1, 2, 2) << 16 | jobc(4, 0, 2, 1, 2) << 32 |
+                             jobc(5, 1, 2, 0, 2) << 48;
+
+// Entry p of the 36 pairs i <= j (row-major): the table offsets of the nine stiffness
+// terms (the formulas of q1Stiffness), their signs, the mass-table offset and cx.
+__device__ uint4 pairDesc(int p)
+{
+  int i = 0;
+  while (p >= 8 - i)
+  {
+    p -= 8 - i;
+    ++i;
+  }
+  int const j = i + p;
+  int const li = i ^ ((i >> 1) & 1), lj = j ^ ((j >> 1) & 1);
+  int const ix = li & 1, iy = (li >> 1) & 1, iz = li >> 2;
+  int const jx = lj & 1, jy = (lj >> 1) & 1, jz = lj >> 2;
+  int const cx = cls(ix, jx), cy = cls(iy, jy), cz = cls(iz, jz);
+  uint32_t const off[9] = {
+      (uint32_t)(0 * 12 + cy * 3 + cz),            (uint32_t)(1 * 12 + cx * 3 + cz),
+      (uint32_t)(2 * 12 + cx * 3 + cy),            (uint32_t)(5 * 12 + (2 * jx + iy) * 3 + cz),
+      (uint32_t)(5 * 12 + (2 * ix + jy) * 3 + cz), (uint32_t)(6 * 12 + (2 * jx + iz) * 3 + cy),
+      (uint32_t)(6 * 12 + (2 * ix + jz) * 3 + cy), (uint32_t)(7 * 12 + (2 * jy + iz) * 3 + cx),
+      (uint32_t)(7 * 12 + (2 * iy + jz) * 3 + cx)};
+  bool const pos[9] = {ix == jx, iy == jy, iz == jz, ix == jy, iy == jx, ix == jz, iz == jx, iy == jz, iz == jy};
+  uint32_t neg = 0;
+  for (int k = 0; k < 9; ++k)
+    neg |= pos[k] ? 0u : 1u << k;
+  uint4 d;
+  d.x = (uint32_t)i | (uint32_t)j << 3 | (uint32_t)cx << 6 | neg << 8;
+  d.y = off[0] | off[1] << 8 | off[2] << 16 | off[3] << 24;
+  d.z = off[4] | off[5] << 8 | off[6] << 16 | off[7] << 24;
+  d.w = off[8] | (uint32_t)(3 * 12 + cy * 3 + cz) << 8;
+  return d;
+}
+
+// Dirichlet condensation of one entry (builder.hpp:76-124): a constrained diagonal
+// takes bcDiag, a free row the lift -K_ij h_j.  Out of line: its FP64 code would
+// otherwise be predicated into every entry.
+__device__ __noinline__ void condenseEntry(double * diag, double bcDiag, double * b, uint32_t dofi, uint32_t dofj,
+                                           double bvi, double bvj, bool ci, bool cj, bool isDiag, double val)
+{
+  if (isDiag)
+  {
+    atomicAdd(diag, bcDiag);
+    return;
+  }
+  if (!b)
+    return;
+  if (!ci)
+  {
+    double const t = val * bvj;
+    if (t != 0.)
+      atomicAdd(b + dofi, -t);
+  }
+  if (!cj)
+  {
+    double const t = val * bvi;
+    if (t != 0.)
+      atomicAdd(b + dofj, -t);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T pick3(T const (&v)[3], int d)
+{
+  return d == 0 ? v[0] : (d == 1 ? v[1] : v[2]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 4) kAssembleQ1Group(AsmArgs a)
+{
+  extern __shared__ uint4 dynShared[]; // ElemShared<T>[kThreads / 8], then the 36 pair descriptors
+  ElemShared<T> * shAll = reinterpret_cast<ElemShared<T> *>(dynShared);
+  uint4 * sDesc = reinterpret_cast<uint4 *>(shAll + kThreads / 8);
+  if (threadIdx.x < 36)
+    sDesc[threadIdx.x] = pairDesc(threadIdx.x);
+  __syncthreads();
+
+  int const l = threadIdx.x & 7;
+  int const g0 = threadIdx.x & 24; // first lane of the group in the warp
+  ElemShared<T> & sh = shAll[threadIdx.x >> 3];
+  int64_t const eg = ((int64_t)blockIdx.x * kThreads + threadIdx.x) >> 3;
+  bool const live = eg < a.nelem;
+  int64_t const e = live ? eg : a.nelem - 1; // a tail group recomputes the last element, writes nothing
+  int const bx = l & 1, by = (l >> 1) & 1, bz = l >> 2;
+  bool const lhs = a.op[0].on || a.op[1].on;
+
+  // ---- node data: lane l = node l
+  uint32_t const dofl = a.emap[8 * e + l];
+  bool const cl = a.bcMask && a.bcMask[dofl];
+  uint32_t const cons = (__ballot_sync(kFull, cl) >> g0) & 0xffu;
+  sh.dof[l] = dofl;
+  sh.bv[l] = (cl && a.bcVal) ? a.bcVal[dofl] : 0.;
+  if (lhs)
+  {
+    sh.rp[l] = a.rowPtr[dofl];
+    reinterpret_cast<uint4 *>(sh.rank)[l] = reinterpret_cast<uint4 const *>(a.rank + 64 * e)[l];
+  }
+
+  // ---- vertex coordinates: lane l = lattice vertex l = node l ^ by, relative to vertex 0
+  uint32_t const vtx = a.conn[8 * e + (l ^ by)];
+  double X0[3];
+  T Y[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    double const x = a.xyz[3 * (int64_t)vtx + d];
+    X0[d] = __shfl_sync(kFull, x, g0);
+    Y[d] = fromDouble<T>(x - X0[d]);
+  }
+  __syncthreads();
+
+  // ---- A. geometry at Gauss point q = l
+  T J[3][3];
+  {
+    T Dx[3], Lx[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+    {
+      T const p = shx(Y[r], 1);
+      Dx[r] = halfSgn(Y[r] - p, bx);
+      Lx[r] = cst<T>(A) * Y[r] + cst<T>(B) * p;
+    }
+    T DxLy[3], LxDy[3], LxLy[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+    {
+      T const pd = shx(Dx[r], 2), pl = shx(Lx[r], 2);
+      DxLy[r] = cst<T>(A) * Dx[r] + cst<T>(B) * pd;
+      LxDy[r] = halfSgn(Lx[r] - pl, by);
+      LxLy[r] = cst<T>(A) * Lx[r] + cst<T>(B) * pl;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+    {
+      T const p1 = shx(DxLy[r], 4), p2 = shx(LxDy[r], 4), p3 = shx(LxLy[r], 4);
+      J[r][0] = cst<T>(A) * DxLy[r] + cst<T>(B) * p1;
+      J[r][1] = cst<T>(A) * LxDy[r] + cst<T>(B) * p2;
+      J[r][2] = halfSgn(LxLy[r] - p3, bz);
+    }
+  }
+  T adet, off[3];
+  {
+    T C[3][3]; // adj(J)
+    C[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    C[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    C[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    C[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    C[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    C[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    C[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    C[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    T const det = J[0][0] * C[0][0] + J[0][1] * C[1][0] + J[0][2] * C[2][0];
+    adet = fabs(det);
+    T const s = cst<T>(0.25) * rcp(adet);
+    sh.u.G[0][l] = s * (C[0][0] * C[0][0] + C[0][1] * C[0][1] + C[0][2] * C[0][2]);
+    sh.u.G[1][l] = s * (C[1][0] * C[1][0] + C[1][1] * C[1][1] + C[1][2] * C[1][2]);
+    sh.u.G[2][l] = s * (C[2][0] * C[2][0] + C[2][1] * C[2][1] + C[2][2] * C[2][2]);
+    sh.u.G[3][l] = s * (C[0][0] * C[1][0] + C[0][1] * C[1][1] + C[0][2] * C[1][2]);
+    sh.u.G[4][l] = s * (C[0][0] * C[2][0] + C[0][1] * C[2][1] + C[0][2] * C[2][2]);
+    sh.u.G[5][l] = s * (C[1][0] * C[2][0] + C[1][1] * C[2][1] + C[1][2] * C[2][2]);
+    sh.u.G[6][l] = adet;
+    T const xq = negIf(cst<T>(g), !bx), yq = negIf(cst<T>(g), !by), zq = negIf(cst<T>(g), !bz);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      off[r] = J[r][0] * xq + J[r][1] * yq + J[r][2] * zq;
+  }
+
+  // ---- D. load vector (and the Dirichlet rows' h, once per operator with bc)
+  bool const anyBc = cons && ((a.op[0].on && a.op[0].bc) || (a.op[1].on && a.op[1].bc));
+  if (a.b)
+  {
+    if (anyBc && live && cl && sh.bv[l] != 0.)
+    {
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+        if (a.op[m].on && a.op[m].bc)
+          atomicAdd(a.b + dofl, sh.bv[l]);
+    }
+    if (a.rkind)
+    {
+      T rq;
+      if (a.rkind == 1)
+      {
+        T sY[3]; // sums of the relative coordinates: centroid = X0 + sY / 8
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+          T v = Y[d] + shx(Y[d], 1);
+          v = v + shx(v, 2);
+          sY[d] = v + shx(v, 4);
+        }
+        if (a.fn == PXG_FN_SIN3)
+        {
+          int const dd = l < 3 ? l : 2;
+          double const od = pick3(X0, dd) + toDouble(scl(pick3(sY, dd), 0.125f));
+          T so, co;
+          sinCosPiG(od, so, co);
+          T f = cst<T>(1.0);
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            f = f * sinpiNear(shs(so, g0 + d), shs(co, g0 + d), __shfl_sync(kFull, od, g0 + d), off[d]);
+          rq = adet * (fromDouble<T>(a.rc) * f);
+        }
+        else
+        {
+          double x[3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            x[d] = X0[d] + toDouble(scl(sY[d], 0.125f)) + toDouble(off[d]);
+          rq = fromDouble<T>(toDouble(adet) * evalFn(a.fn, a.rc, x[0], x[1], x[2]));
+        }
+      }
+      else
+      {
+        // projection of a DOF field: node values -> Gauss point
+        T v = fromDouble<T>(a.field[sh.dof[l ^ by]]);
+        v = lerp2(v, 1);
+        v = lerp2(v, 2);
+        v = lerp2(v, 4);
+        rq = adet * (fromDouble<T>(a.rc) * v);
+      }
+      T F = lerp2(rq, 1);
+      F = lerp2(F, 2);
+      F = lerp2(F, 4);
+      int const n = l ^ by;
+      if (live && !(a.rbc && ((cons >> n) & 1u)))
+        atomicAdd(a.b + sh.dof[n], toDouble(F));
+    }
+  }
+  if (!lhs)
+    return; // uniform over the block: the kernel arguments
+
+  // ---- B. tables, lane l = job l
+  __syncthreads();
+  {
+    uint32_t const code = (uint32_t)((l < 4 ? kJobsLo : kJobsHi) >> (16 * (l & 3))) & 0x7ffu;
+    int const cmp = code & 7, su = 1 << ((code >> 3) & 3), sv = 1 << ((code >> 5) & 3), sw = 1 << ((code >> 7) & 3);
+    int const kind = code >> 9;
+    T F[2][2][2]; // [qw][qv][qu]
+#pragma unroll
+    for (int qw = 0; qw < 2; ++qw)
+#pragma unroll
+      for (int qv = 0; qv < 2; ++qv)
+#pragma unroll
+        for (int qu = 0; qu < 2; ++qu)
+          F[qw][qv][qu] = sh.u.G[cmp][qu * su + qv * sv + qw * sw];
+    __syncthreads(); // the tables overwrite G
+    bool const isU = kind == 2;
+    T const a0 = isU ? cst<T>(A) : cst<T>(1.0);
+    T const a1 = isU ? cst<T>(B) : (kind == 1 ? cst<T>(-1.0) : cst<T>(1.0));
+    T P0[2][2], P1[2][2]; // [qw][qv]: along u with (a0, a1), and with l_1 (U jobs)
+#pragma unroll
+    for (int qw = 0; qw < 2; ++qw)
+#pragma unroll
+      for (int qv = 0; qv < 2; ++qv)
+      {
+        P0[qw][qv] = a0 * F[qw][qv][0] + a1 * F[qw][qv][1];
+        P1[qw][qv] = cst<T>(B) * F[qw][qv][0] + cst<T>(A) * F[qw][qv][1];
+      }
+    // row r along v: classes W_r (sum jobs, r < 3) or l_(r & 1) of P0 / P1 (U jobs)
+    constexpr double kS0[4] = {AA, BB, AB, 0.}, kS1[4] = {BB, AA, AB, 0.};
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+    {
+      T const x0 = isU ? cst<T>((r & 1) ? B : A) : cst<T>(kS0[r]);
+      T const x1 = isU ? cst<T>((r & 1) ? A : B) : cst<T>(kS1[r]);
+      T R[2];
+#pragma unroll
+      for (int qw = 0; qw < 2; ++qw)
+      {
+        T const s0 = (r >= 2 && isU) ? P1[qw][0] : P0[qw][0];
+        T const s1 = (r >= 2 && isU) ? P1[qw][1] : P0[qw][1];
+        R[qw] = x0 * s0 + x1 * s1;
+      }
+      // classes along w
+      T const sum = R[0] + R[1], dif = R[0] - R[1];
+      T const as = cst<T>(kAlpha01) * sum, bd = cst<T>(kBeta0) * dif;
+      sh.u.tab[l * 12 + r * 3 + 0] = as + bd;
+      sh.u.tab[l * 12 + r * 3 + 1] = as - bd;
+      sh.u.tab[l * 12 + r * 3 + 2] = cst<T>(AB) * sum;
+    }
+  }
+  __syncthreads();
+
+  // ---- C. entries, lane l = pairs l, l + 8, ...
+  bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
+  bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
+  double const kfac = a.kE ? a.kE[e] : 1.0;
+  T ks[2], ms[2];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+  {
+    LhsDev const & op = a.op[m];
+    ks[m] = fromDouble<T>(op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.);
+    ms[m] = fromDouble<T>(op.mass ? op.mc : 0.);
+  }
+  T const * tb = sh.u.tab;
+  for (int k = 0; k < 5; ++k)
+  {
+    int const p = l + 8 * k;
+    if (p >= 36)
+      break;
+    uint4 const d = sDesc[p];
+    int const i = d.x & 7, j = (d.x >> 3) & 7, cx = (d.x >> 6) & 3;
+    uint32_t const neg = d.x >> 8;
+    T kv = cst<T>(0.0), mv = cst<T>(0.0);
+    if (needK)
+    {
+      kv = negIf(tb[d.y & 0xffu], neg & 1u);
+      kv = kv + negIf(tb[(d.y >> 8) & 0xffu], (neg >> 1) & 1u);
+      kv = kv + negIf(tb[(d.y >> 16) & 0xffu], (neg >> 2) & 1u);
+      kv = kv + negIf(tb[d.y >> 24], (neg >> 3) & 1u);
+      kv = kv + negIf(tb[d.z & 0xffu], (neg >> 4) & 1u);
+      kv = kv + negIf(tb[(d.z >> 8) & 0xffu], (neg >> 5) & 1u);
+      kv = kv + negIf(tb[(d.z >> 16) & 0xffu], (neg >> 6) & 1u);
+      kv = kv + negIf(tb[d.z >> 24], (neg >> 7) & 1u);
+      kv = kv + negIf(tb[d.w & 0xffu], (neg >> 8) & 1u);
+    }
+    if (needM)
+    {
+      uint32_t const mo = d.w >> 8;
+      T const alpha = cx == 2 ? cst<T>(AB) : cst<T>(kAlpha01);
+      T const beta = negIf(cx == 2 ? cst<T>(0.0) : cst<T>(kBeta0), cx == 1);
+      mv = alpha * tb[mo] + beta * tb[mo + 12];
+    }
+    bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+    {
+      LhsDev const & op = a.op[m];
+      if (!op.on)
+        continue;
+      T const v = op.stiff ? (op.mass ? ks[m] * kv + ms[m] * mv : ks[m] * kv) : ms[m] * mv;
+      double const val = toDouble(v);
+      if (!live)
+        continue;
+      if (anyBc && op.bc && (ci || cj))
+      {
+        condenseEntry(op.vals + sh.rp[i] + sh.rank[i * 9], a.bcDiag, a.b, sh.dof[i], sh.dof[j], sh.bv[i], sh.bv[j],
+                      ci, cj, i == j, val);
+        continue;
+      }
+      atomicAdd(op.vals + sh.rp[i] + sh.rank[i * 8 + j], val);
+      if (i != j)
+        atomicAdd(op.vals + sh.rp[j] + sh.rank[j * 8 + i], val);
+    }
+  }
+}
+} // namespace q1g
+
+void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread)
+{
+  if (perThread)
+  {
+    unsigned const blocks = (unsigned)((a.nelem + 127) / 128);
+    if (fp64)
+      kAssembleQ1<double><<<blocks, 128, 0, s>>>(a);
+    else
+      kAssembleQ1<dfl><<<blocks, 128, 0, s>>>(a);
+    return;
+  }
+  unsigned const blocks = (unsigned)((a.nelem * 8 + q1g::kThreads - 1) / q1g::kThreads);
   if (fp64)
-    kAssembleQ1<double><<<blocks, 128, 0, s>>>(a);
+    q1g::kAssembleQ1Group<double><<<blocks, q1g::kThreads, q1g::kSmemBytes, s>>>(a);
   else
-    kAssembleQ1<dfl><<<blocks, 128, 0, s>>>(a);
+    q1g::kAssembleQ1Group<dfl><<<blocks, q1g::kThreads, q1g::kSmemBytes, s>>>(a);
 }
 
 // Adjoint gradient g_e = -(C u)_e^T K_e (C lambda)_e, K_e = k_e K0_e (Q1, 2x2x2 rule):

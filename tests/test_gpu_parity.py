@@ -61,6 +61,14 @@ def test_prune_cancellation_margin(engine):
     assert compare_csr(g["mats"][0], csr, ndof) == 0  # bit-exact pruned pattern
     near = (sv > 1e-18) & (sv < 1e-14)
     assert not near.any(), f"{near.sum()} entries near the prune threshold"
+    # the synchronous and the stream-ordered prune counts agree with the compaction
+    import torch
+
+    v = torch.as_tensor(g["struct_vals"][0]).cuda()
+    out = torch.full((2,), -1, dtype=torch.int64, device="cuda")
+    g["ctx"].prune_count_device(v, out[1:])
+    assert g["ctx"].prune_count(v) == out[1].item() == nz - g["mats"][0][1].size
+    assert out[0].item() == -1
 
 
 @pytest.mark.parametrize("t,gen", [(O.P1TET, "tet6"), (O.P2TET, "tet5"), (O.Q1HEX, "hex"), (O.Q2HEX, "hex")])
@@ -144,17 +152,19 @@ def test_invalid_inputs_rejected(engine):
     assert torch.isfinite(v).all()
 
 
-@pytest.mark.parametrize("kernel", ["dfl", "fp64", "generic"])
+@pytest.mark.parametrize("kernel", ["dfl", "fp64", "thread-dfl", "thread-fp64", "generic"])
 @pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
 @pytest.mark.parametrize("n", [7, 40])
 def test_q1_kernels_agree_with_oracle(engine, monkeypatch, kernel, bc, n):
-    """The three Q1 kernels against the oracle: the tensor-product kernel in
-    double-float arithmetic (default), its FP64 variant, and the generic kernel;
-    K(k_e) + M + sin3 load on a perturbed mesh, with and without inhomogeneous
-    Dirichlet data.  n = 40 takes the short-series path of the load (small offsets),
-    n = 7 the direct sinpi path."""
+    """The Q1 kernels against the oracle: the eight-lanes-per-element tensor-product
+    kernel in double-float arithmetic (default) and in FP64, the one-thread-per-element
+    kernel in both arithmetics, and the generic kernel; K(k_e) + M + sin3 load on a
+    perturbed mesh, with and without inhomogeneous Dirichlet data.  n = 40 takes the
+    short-series path of the load (small offsets), n = 7 the direct sinpi path; 7^3
+    elements also leave a partly filled last block."""
     monkeypatch.setenv("PXG_Q1_GENERIC", "1" if kernel == "generic" else "0")
-    monkeypatch.setenv("PXG_Q1_FP64", "1" if kernel == "fp64" else "0")
+    monkeypatch.setenv("PXG_Q1_FP64", "1" if kernel.endswith("fp64") else "0")
+    monkeypatch.setenv("PXG_Q1_THREAD", "1" if kernel.startswith("thread") else "0")
     xyz, conn, k = problem("hex", n, 0.2, seed=21, sigma=1.0)
     em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
     bcarg, mask, val = None, None, None
