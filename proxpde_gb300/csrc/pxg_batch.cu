@@ -18,6 +18,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -66,6 +67,7 @@ struct SysDev
   double * w;
   double * Mw;
   int64_t nrows;
+  int shortRows; // 1: rows of at most 16 entries (2 lanes per row in the products)
 };
 
 struct BatchDev
@@ -83,7 +85,33 @@ struct BatchDev
   unsigned extra; // arrivals expected beyond the grid (0; >0 only to test the timeout path)
   double tol2;
   int maxIter;
+  // problem table and the chunk tables of alternate iterations
+  int const * probSys;
+  int64_t const * probRow0;
+  int64_t const * probRows;
+  int * chunkProb[2];
+  int64_t * chunkRow0[2];
+  int * chunkRows[2];
+  int * nchunk; // [2]
+  // optional timeline (PXG_BATCH_TRACE): per CG iteration the global timer after each
+  // phase and the chunk count, written by block 0; nullptr when off
+  unsigned long long * trace;
+  int traceCap;
 };
+
+__device__ __forceinline__ unsigned long long globalTimer()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// record slot k of the timeline (block 0, thread 0)
+__device__ __forceinline__ void traceMark(BatchDev const & d, int k, unsigned long long v)
+{
+  if (d.trace && blockIdx.x == 0 && threadIdx.x == 0 && k < d.traceCap)
+    d.trace[k] = v;
+}
 
 // Grid barrier with a bounded wait.  Returns false (and sets err) on timeout.
 __device__ bool gridSync(BatchDev const & d)
@@ -245,16 +273,139 @@ __device__ __forceinline__ void blockRows(BatchDev const & d, int64_t & r0, int6
     r1 = d.total;
 }
 
+// Sum NV per-thread values over the block and add them to dst[slot[q]] (one atomic
+// per quantity).  Every thread of the block calls it.
+template <int NV>
+__device__ __forceinline__ void blockAddTo(double (&v)[NV], double * dst, int const (&slot)[NV])
+{
+  __shared__ double red[kBt / 32][NV];
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+  {
+    double x = v[q];
+    for (int o = 16; o > 0; o >>= 1)
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0)
+      red[warp][q] = x;
+  }
+  __syncthreads();
+  if (warp == 0)
+  {
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+    {
+      double x = lane < kBt / 32 ? red[lane][q] : 0.;
+      for (int o = 16; o > 0; o >>= 1)
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0 && x != 0.)
+        atomicAdd(dst + slot[q], x);
+    }
+  }
+  __syncthreads();
+}
+
+// Exclusive prefix sum over the block of one int per thread; returns the thread's
+// offset and sets total.  Every thread of the block calls it.
+__device__ __forceinline__ int blockExclusiveScan(int x, int & total)
+{
+  __shared__ int wsum[kBt / 32];
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inc = x;
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    int const y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o)
+      inc += y;
+  }
+  if (lane == 31)
+    wsum[warp] = inc;
+  __syncthreads();
+  int base = 0, tot = 0;
+  for (int w = 0; w < kBt / 32; ++w)
+  {
+    base += w < warp ? wsum[w] : 0;
+    tot += wsum[w];
+  }
+  __syncthreads();
+  total = tot;
+  return base + inc - x;
+}
+
+// Block 0: cut the rows of the running problems into chunks of equal size (at least
+// 256 rows, about eight per block) for the iterations of parity `par`.  The chunks are
+// dealt round-robin to the blocks, so the work of an iteration follows the running
+// problems instead of a fixed row partition.
+__device__ void buildChunks(BatchDev const & d, int par)
+{
+  __shared__ long long sRows;
+  if (threadIdx.x == 0)
+    sRows = 0;
+  __syncthreads();
+  long long mine = 0;
+  for (int k = threadIdx.x; k < d.nprob; k += blockDim.x)
+    if (!__ldcg(d.done + k))
+      mine += d.probRows[k];
+  atomicAdd(reinterpret_cast<unsigned long long *>(&sRows), (unsigned long long)mine);
+  __syncthreads();
+  long long const rows = sRows;
+  long long csize = (rows + 8ll * gridDim.x - 1) / (8ll * gridDim.x);
+  csize = csize < 256 ? 256 : csize;
+  int running = 0;
+  for (int base = 0; base < d.nprob; base += blockDim.x)
+  {
+    int const k = base + threadIdx.x;
+    int64_t const nr = (k < d.nprob && !__ldcg(d.done + k)) ? d.probRows[k] : 0;
+    int const nc = (int)((nr + csize - 1) / csize);
+    int tot;
+    int const off = running + blockExclusiveScan(nc, tot);
+    for (int c = 0; c < nc; ++c)
+    {
+      d.chunkProb[par][off + c] = k;
+      d.chunkRow0[par][off + c] = d.probRow0[k] + c * csize;
+      d.chunkRows[par][off + c] = (int)(nr - c * csize < csize ? nr - c * csize : csize);
+    }
+    running += tot;
+  }
+  if (threadIdx.x == 0)
+    d.nchunk[par] = running;
+  __threadfence();
+}
+
+// q = K p over the rows [c0, c0 + nr) of one chunk; returns the thread's share of p.q
+template <int LPR, int UNR>
+__device__ __forceinline__ double spmvChunk(SysDev const & s, int64_t c0, int nr)
+{
+  constexpr int RPW = 32 / LPR;
+  int const lane = threadIdx.x & 31, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
+  double pq = 0.;
+  for (int v0 = warp * RPW; v0 < nr; v0 += nwarps * RPW)
+  {
+    int const v = v0 + lane / LPR;
+    bool const act = v < nr;
+    int64_t const lr = c0 + (act ? v : 0);
+    double const t = rowDot<true, LPR, UNR>(s.rp, s.ci, s.K, s.p, lr, act);
+    if (act && (lane & (LPR - 1)) == 0)
+    {
+      __stcg(s.q + lr, t);
+      pq += __ldcg(s.p + lr) * t;
+    }
+  }
+  return pq;
+}
+
+constexpr int kRu = 4;  // rows per thread whose loads are issued before any store (p update)
+constexpr int kRu2 = 2; // the same for the x, r, z update (five loads a row)
+
 // One batched PCG solve: x = K^-1 rhs per problem.  `forward` selects (b -> u) or
 // (Mw -> lam).  Returns false on a barrier timeout.
-__device__ bool batchCg(BatchDev const & d, bool forward, BlockAcc<2> & ba2, BlockAcc<1> & ba1)
+__device__ bool batchCg(BatchDev const & d, bool forward, BlockAcc<2> & ba2)
 {
+  int const tb = forward ? 0 : d.traceCap / 2; // timeline: [iteration][S1 end, S2 end, S3 end, chunks]
   int64_t const nthr = (int64_t)gridDim.x * blockDim.x;
   int64_t const tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t r0, r1;
   blockRows(d, r0, r1);
-  constexpr int RPW = 32 / kLpr;
-  int const lane = threadIdx.x & 31, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
   // reset accumulators and flags
   for (int64_t k = tid; k < (int64_t)d.nprob * A_N; k += nthr)
     if ((k % A_N) != A_J)
@@ -294,14 +445,26 @@ __device__ bool batchCg(BatchDev const & d, bool forward, BlockAcc<2> & ba2, Blo
   }
   if (!gridSync(d))
     return false;
-  for (int64_t k = tid; k < d.nprob; k += nthr)
-    if (d.acc[k * A_N + A_BB] == 0.)
-      d.done[k] = 1;
+  if (blockIdx.x == 0)
+  {
+    for (int k = threadIdx.x; k < d.nprob; k += blockDim.x)
+      if (__ldcg(d.acc + (int64_t)k * A_N + A_BB) == 0.)
+        d.done[k] = 1;
+    __syncthreads();
+    buildChunks(d, 0);
+  }
   if (!gridSync(d))
     return false;
+  traceMark(d, d.traceCap / 2 - 1 + tb, globalTimer()); // start of the iterations
   for (int it = 0; it < d.maxIter; ++it)
   {
     int const par = it & 1;
+    int const nch = __ldcg(d.nchunk + par);
+    if (nch == 0)
+      break; // every problem has converged
+    int const * cProb = d.chunkProb[par];
+    int64_t const * cRow0 = d.chunkRow0[par];
+    int const * cRows = d.chunkRows[par];
     // S1: q = K p, p.q ; zero the slots reused next
     if (blockIdx.x == 0)
       for (int k = threadIdx.x; k < d.nprob; k += blockDim.x)
@@ -310,79 +473,103 @@ __device__ bool batchCg(BatchDev const & d, bool forward, BlockAcc<2> & ba2, Blo
         d.acc[(int64_t)k * A_N + A_RR0 + (par ^ 1)] = 0.;
         d.acc[(int64_t)k * A_N + A_RZ0 + par] = 0.;
       }
+    for (int c = blockIdx.x; c < nch; c += gridDim.x)
     {
+      int const pr = __ldcg(cProb + c);
+      int64_t const c0 = __ldcg(cRow0 + c);
+      int const nr = __ldcg(cRows + c);
+      SysDev const & s = d.sys[d.probSys[pr]];
+      double pq[1] = {s.shortRows ? spmvChunk<2, 8>(s, c0, nr) : spmvChunk<4, 7>(s, c0, nr)};
       int const sl[1] = {A_PQ0 + par};
-      baBegin<1>(ba1, d, r0, r1);
-      LaneAcc<1> la;
-      for (int64_t g0 = r0 + (int64_t)warp * RPW; g0 < r1; g0 += (int64_t)nwarps * RPW)
-      {
-        int64_t const g = g0 + lane / kLpr;
-        int64_t lr = 0;
-        int sy = 0, pr = -1;
-        bool act = false;
-        if (g < r1)
-        {
-          sy = sysOf(d, g, lr);
-          pr = d.sys[sy].rowProb[lr];
-          act = !__ldcg(d.done + pr);
-        }
-        SysDev const & s = d.sys[sy];
-        double const t = rowDot<true>(s.rp, s.ci, s.K, s.p, lr, act);
-        if (act && (lane & (kLpr - 1)) == 0)
-        {
-          __stcg(s.q + lr, t);
-          double const v[1] = {__ldcg(s.p + lr) * t};
-          laAdd<1>(la, ba1, d.acc, sl, pr, v);
-        }
-      }
-      baEnd<1>(ba1, la, d.acc, sl);
+      blockAddTo<1>(pq, d.acc + (int64_t)pr * A_N, sl);
     }
     if (!gridSync(d))
       return false;
+    if (4 * it + 3 < d.traceCap / 2 - 1)
+      traceMark(d, tb + 4 * it, globalTimer());
     // S2: x += alpha p, r -= alpha q, z = D^-1 r ; r.z, r.r
+    for (int c = blockIdx.x; c < nch; c += gridDim.x)
     {
-      int const sl[2] = {A_RZ0 + par, A_RR0 + par};
-      baBegin<2>(ba2, d, r0, r1);
-      LaneAcc<2> la;
-      for (int64_t g = r0 + threadIdx.x; g < r1; g += blockDim.x)
+      int const pr = __ldcg(cProb + c);
+      int64_t const c0 = __ldcg(cRow0 + c);
+      int const nr = __ldcg(cRows + c);
+      SysDev const & s = d.sys[d.probSys[pr]];
+      double const * a = d.acc + (int64_t)pr * A_N;
+      double const al = __ldcg(a + A_RZ0 + (par ^ 1)) / __ldcg(a + A_PQ0 + par);
+      double * x = forward ? s.u : s.lam;
+      double v2[2] = {0., 0.};
+      for (int v = threadIdx.x; v < nr; v += kRu2 * blockDim.x)
       {
-        int64_t lr;
-        SysDev const & s = d.sys[sysOf(d, g, lr)];
-        int const pr = s.rowProb[lr];
-        if (__ldcg(d.done + pr))
-          continue;
-        double const * a = d.acc + (int64_t)pr * A_N;
-        double const al = __ldcg(a + A_RZ0 + (par ^ 1)) / __ldcg(a + A_PQ0 + par);
-        double * x = forward ? s.u : s.lam;
-        __stcg(x + lr, __ldcg(x + lr) + al * __ldcg(s.p + lr));
-        double const ri = __ldcg(s.r + lr) - al * __ldcg(s.q + lr);
-        __stcg(s.r + lr, ri);
-        double const zi = s.dinv[lr] * ri;
-        __stcg(s.z + lr, zi);
-        double const v[2] = {ri * zi, ri * ri};
-        laAdd<2>(la, ba2, d.acc, sl, pr, v);
+        double xv[kRu2], pv[kRu2], rv[kRu2], qv[kRu2], dv[kRu2];
+#pragma unroll
+        for (int u = 0; u < kRu2; ++u)
+        {
+          int const vv = v + u * blockDim.x;
+          int64_t const lr = c0 + (vv < nr ? vv : 0);
+          xv[u] = __ldcg(x + lr);
+          pv[u] = __ldcg(s.p + lr);
+          rv[u] = __ldcg(s.r + lr);
+          qv[u] = __ldcg(s.q + lr);
+          dv[u] = s.dinv[lr];
+        }
+#pragma unroll
+        for (int u = 0; u < kRu2; ++u)
+        {
+          int const vv = v + u * blockDim.x;
+          if (vv >= nr)
+            break;
+          int64_t const lr = c0 + vv;
+          __stcg(x + lr, xv[u] + al * pv[u]);
+          double const ri = rv[u] - al * qv[u];
+          __stcg(s.r + lr, ri);
+          double const zi = dv[u] * ri;
+          __stcg(s.z + lr, zi);
+          v2[0] += ri * zi;
+          v2[1] += ri * ri;
+        }
       }
-      baEnd<2>(ba2, la, d.acc, sl);
+      int const sl[2] = {A_RZ0 + par, A_RR0 + par};
+      blockAddTo<2>(v2, d.acc + (int64_t)pr * A_N, sl);
     }
     if (!gridSync(d))
       return false;
+    if (4 * it + 3 < d.traceCap / 2 - 1)
+      traceMark(d, tb + 4 * it + 1, globalTimer());
     // S3: convergence per problem, p = z + beta p
-    for (int64_t g = r0 + threadIdx.x; g < r1; g += blockDim.x)
+    for (int c = blockIdx.x; c < nch; c += gridDim.x)
     {
-      int64_t lr;
-      SysDev const & s = d.sys[sysOf(d, g, lr)];
-      int const pr = s.rowProb[lr];
-      if (__ldcg(d.done + pr))
-        continue;
+      int const pr = __ldcg(cProb + c);
       double const * a = d.acc + (int64_t)pr * A_N;
-      if (!(__ldcg(a + A_RR0 + par) <= d.tol2 * __ldcg(a + A_BB)))
+      if (__ldcg(a + A_RR0 + par) <= d.tol2 * __ldcg(a + A_BB))
+        continue;
+      int64_t const c0 = __ldcg(cRow0 + c);
+      int const nr = __ldcg(cRows + c);
+      SysDev const & s = d.sys[d.probSys[pr]];
+      double const be = __ldcg(a + A_RZ0 + par) / __ldcg(a + A_RZ0 + (par ^ 1));
+      for (int v = threadIdx.x; v < nr; v += kRu * blockDim.x)
       {
-        double const be = __ldcg(a + A_RZ0 + par) / __ldcg(a + A_RZ0 + (par ^ 1));
-        __stcg(s.p + lr, __ldcg(s.z + lr) + be * __ldcg(s.p + lr));
+        double zv[kRu], pv[kRu];
+#pragma unroll
+        for (int u = 0; u < kRu; ++u)
+        {
+          int const vv = v + u * blockDim.x;
+          int64_t const lr = c0 + (vv < nr ? vv : 0);
+          zv[u] = __ldcg(s.z + lr);
+          pv[u] = __ldcg(s.p + lr);
+        }
+#pragma unroll
+        for (int u = 0; u < kRu; ++u)
+        {
+          int const vv = v + u * blockDim.x;
+          if (vv < nr)
+            __stcg(s.p + c0 + vv, zv[u] + be * pv[u]);
+        }
       }
     }
-    // bookkeeping by block 0 (other blocks only read `done` after the barrier)
+    // bookkeeping and the next iteration's chunks, by block 0 (the other blocks read
+    // them after the barrier)
     if (blockIdx.x == 0)
+    {
       for (int k = threadIdx.x; k < d.nprob; k += blockDim.x)
         if (!d.done[k])
         {
@@ -393,28 +580,25 @@ __device__ bool batchCg(BatchDev const & d, bool forward, BlockAcc<2> & ba2, Blo
             (forward ? d.itF : d.itA)[k] = it + 1;
           }
         }
+      __syncthreads();
+      buildChunks(d, par ^ 1);
+    }
     if (!gridSync(d))
       return false;
-    // all problems done?
-    __shared__ int running;
-    if (threadIdx.x == 0)
-      running = 0;
-    __syncthreads();
-    for (int k = threadIdx.x; k < d.nprob; k += blockDim.x)
-      if (!__ldcg(d.done + k))
-        running = 1;
-    __syncthreads();
-    if (!running)
-      break;
+    if (4 * it + 3 < d.traceCap / 2 - 1)
+    {
+      traceMark(d, tb + 4 * it + 2, globalTimer());
+      traceMark(d, tb + 4 * it + 3, (unsigned long long)nch);
+    }
   }
   return gridSync(d);
 }
 
-__global__ void __launch_bounds__(kBt) kBatchSolve(BatchDev d)
+__global__ void __launch_bounds__(kBt, 4) kBatchSolve(BatchDev d)
 {
   __shared__ BlockAcc<2> ba2;
   __shared__ BlockAcc<1> ba1;
-  if (!batchCg(d, true, ba2, ba1))
+  if (!batchCg(d, true, ba2))
     return;
   // loss: w = u - u_t, Mw = M w, J_p = 1/2 w.Mw
   int64_t r0, r1;
@@ -454,7 +638,7 @@ __global__ void __launch_bounds__(kBt) kBatchSolve(BatchDev d)
   }
   if (!gridSync(d))
     return;
-  batchCg(d, false, ba2, ba1);
+  batchCg(d, false, ba2);
 }
 
 // DOF range of problem p: from the DOF of its first element's first slot (the first
@@ -548,15 +732,58 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
   int nprob = 0;
   for (int i = 0; i < nctx; ++i)
     nprob += (int)ctxs[i]->batch.nprob;
+  int64_t totalRows = 0;
+  for (int i = 0; i < nctx; ++i)
+    totalRows += ctxs[i]->ndof;
+  int64_t const capChunks = totalRows / 256 + nprob + 16;
+  auto dropGraph = [&] {
+    if (S.exec)
+      cudaGraphExecDestroy(S.exec);
+    S.exec = nullptr;
+  };
   if (S.nprob < nprob)
   {
+    dropGraph(); // the graph holds the old buffers
     PXG_CUDA(c0, S.acc.alloc((size_t)nprob * A_N));
     PXG_CUDA(c0, S.done.alloc(nprob));
     PXG_CUDA(c0, S.itF.alloc(nprob));
     PXG_CUDA(c0, S.itA.alloc(nprob));
     PXG_CUDA(c0, S.bar.alloc(2));
     PXG_CUDA(c0, S.err.alloc(1));
+    PXG_CUDA(c0, S.probSys.alloc(nprob));
+    PXG_CUDA(c0, S.probRow0.alloc(nprob));
+    PXG_CUDA(c0, S.probRows.alloc(nprob));
     S.nprob = nprob;
+  }
+  if (S.capChunks < capChunks)
+  {
+    dropGraph();
+    for (int k = 0; k < 2; ++k)
+    {
+      PXG_CUDA(c0, S.chunkProb[k].alloc(capChunks));
+      PXG_CUDA(c0, S.chunkRows[k].alloc(capChunks));
+      PXG_CUDA(c0, S.chunkRow0[k].alloc(capChunks));
+    }
+    PXG_CUDA(c0, S.nchunk.alloc(2));
+    S.capChunks = capChunks;
+  }
+  {
+    // problem table: system, first row and rows of every problem, in global order
+    std::vector<int> ps;
+    std::vector<int64_t> p0, pn;
+    for (int i = 0; i < nctx; ++i)
+    {
+      std::vector<int64_t> const & off = ctxs[i]->batch.dofOffHost;
+      for (int64_t q = 0; q < ctxs[i]->batch.nprob; ++q)
+      {
+        ps.push_back(i);
+        p0.push_back(off[q]);
+        pn.push_back(off[q + 1] - off[q]);
+      }
+    }
+    PXG_CUDA(c0, cudaMemcpy(S.probSys.p, ps.data(), ps.size() * sizeof(int), cudaMemcpyHostToDevice));
+    PXG_CUDA(c0, cudaMemcpy(S.probRow0.p, p0.data(), p0.size() * 8, cudaMemcpyHostToDevice));
+    PXG_CUDA(c0, cudaMemcpy(S.probRows.p, pn.data(), pn.size() * 8, cudaMemcpyHostToDevice));
   }
   // second batch: its problems follow the first one's
   if (nctx == 2)
@@ -584,7 +811,7 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
     pxg_ctx * c = ctxs[i];
     BatchState & B = c->batch;
     d.sys[i] = SysDev{c->rowPtr.p, c->colIdx.p, B.K.p, B.M.p, B.b.p, u_targets[i], B.rowProb.p, B.u.p, B.lam.p,
-                      B.r.p, B.z.p, B.p.p, B.q.p, B.dinv.p, B.w.p, B.Mw.p, c->ndof};
+                      B.r.p, B.z.p, B.p.p, B.q.p, B.dinv.p, B.w.p, B.Mw.p, c->ndof, c->maxRowLen <= 16 ? 1 : 0};
     d.total += c->ndof;
   }
   d.nprob = nprob;
@@ -596,6 +823,28 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
   d.err = S.err.p;
   d.tol2 = rtol * rtol;
   d.maxIter = max_iter;
+  d.probSys = S.probSys.p;
+  d.probRow0 = S.probRow0.p;
+  d.probRows = S.probRows.p;
+  for (int k = 0; k < 2; ++k)
+  {
+    d.chunkProb[k] = S.chunkProb[k].p;
+    d.chunkRow0[k] = S.chunkRow0[k].p;
+    d.chunkRows[k] = S.chunkRows[k].p;
+  }
+  d.nchunk = S.nchunk.p;
+  // optional timeline of the persistent solver (not with graph replay: the buffer is
+  // read back after the launch)
+  char const * traceFile = getenv("PXG_BATCH_TRACE");
+  DevBuf<unsigned long long> trace;
+  if (traceFile && traceFile[0])
+  {
+    d.traceCap = 2 * (4 * std::min(max_iter, 4096) + 1);
+    PXG_CUDA(c0, trace.alloc(d.traceCap));
+    PXG_CUDA(c0, cudaMemset(trace.p, 0, d.traceCap * 8));
+    d.trace = trace.p;
+    use_graph = 0;
+  }
   {
     // PXG_TEST_BARRIER_SHORTFALL=1 makes every grid barrier wait for one block more
     // than the grid has, so the bounded waits run out (tests of the timeout path)
@@ -695,6 +944,27 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
   PXG_CUDA(c0, cudaStreamSynchronize(s));
   if (err)
     return fail(c0, PXG_ERR_TIMEOUT, "persistent batch solver: a grid barrier wait ran out");
+  if (d.trace)
+  {
+    // text: one line per CG iteration, "solve iteration ns_S1 ns_S2 ns_S3 chunks"
+    std::vector<unsigned long long> t(d.traceCap);
+    PXG_CUDA(c0, cudaMemcpy(t.data(), d.trace, t.size() * 8, cudaMemcpyDeviceToHost));
+    if (FILE * f = fopen(traceFile, "a"))
+    {
+      int const half = d.traceCap / 2;
+      for (int sv = 0; sv < 2; ++sv)
+      {
+        unsigned long long prev = t[sv * half + half - 1];
+        for (int it = 0; 4 * it + 3 < half - 1 && t[sv * half + 4 * it + 2]; ++it)
+        {
+          unsigned long long const * r = &t[sv * half + 4 * it];
+          fprintf(f, "%d %d %llu %llu %llu %llu\n", sv, it, r[0] - prev, r[1] - r[0], r[2] - r[1], r[3]);
+          prev = r[2];
+        }
+      }
+      fclose(f);
+    }
+  }
   int worst = 0;
   bool conv = true;
   for (int p = 0; p < nprob; ++p)

@@ -248,6 +248,13 @@ struct BatchShared
   pxg::DevBuf<double> acc;
   pxg::DevBuf<int> done, itF, itA, err;
   pxg::DevBuf<unsigned> bar;
+  // problem table (global problem id -> system, first row, rows) and the per-iteration
+  // row chunks of the running problems, two tables used by alternate iterations
+  pxg::DevBuf<int> probSys;
+  pxg::DevBuf<int64_t> probRow0, probRows;
+  int64_t capChunks = 0;
+  pxg::DevBuf<int> chunkProb[2], chunkRows[2], nchunk;
+  pxg::DevBuf<int64_t> chunkRow0[2];
   cudaGraphExec_t exec = nullptr;
   GraphKey key;
   ~BatchShared()
@@ -352,38 +359,42 @@ namespace pxg
 {
 constexpr int kLpr = 4;  // lanes per row
 constexpr int kUnr = 8;  // entries per lane and load round
-template <bool L2ONLY>
+// LPR lanes per row (a power of two), UNR entries per lane and round.  The FP64 pipe
+// issues every slot of a round, used or not (GB300: 1/64 of the FP32 rate), so LPR x
+// UNR should just cover the typical row: 4 x 7 for Q1 hexahedra (27 entries), 2 x 8
+// for P1 tetrahedra (15).
+template <bool L2ONLY, int LPR = kLpr, int UNR = kUnr>
 __device__ __forceinline__ double rowDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
                                          double const * __restrict__ a, double const * x, int64_t row, bool valid)
 {
-  // kUnr strided entries per lane and round: their column ids and values are loaded
+  // UNR strided entries per lane and round: their column ids and values are loaded
   // together, then the gathers, so each lane keeps many loads in flight (a row of up
-  // to kLpr * kUnr = 32 entries takes one round)
-  int const sub = threadIdx.x & (kLpr - 1);
+  // to LPR * UNR entries takes one round)
+  int const sub = threadIdx.x & (LPR - 1);
   double t = 0.;
   if (valid)
   {
     int32_t const e = rp[row + 1];
-    for (int32_t base = rp[row] + sub; base < e; base += kUnr * kLpr)
+    for (int32_t base = rp[row] + sub; base < e; base += UNR * LPR)
     {
-      int32_t cc[kUnr];
-      double av[kUnr];
+      int32_t cc[UNR];
+      double av[UNR];
 #pragma unroll
-      for (int u = 0; u < kUnr; ++u)
+      for (int u = 0; u < UNR; ++u)
       {
-        int32_t const k = base + u * kLpr;
+        int32_t const k = base + u * LPR;
         bool const ok = k < e;
         cc[u] = ok ? ci[k] : -1;
         av[u] = ok ? a[k] : 0.;
       }
 #pragma unroll
-      for (int u = 0; u < kUnr; ++u)
+      for (int u = 0; u < UNR; ++u)
         if (cc[u] >= 0)
           t = fma(av[u], L2ONLY ? __ldcg(x + cc[u]) : x[cc[u]], t);
     }
   }
 #pragma unroll
-  for (int o = kLpr / 2; o > 0; o >>= 1)
+  for (int o = LPR / 2; o > 0; o >>= 1)
     t += __shfl_xor_sync(0xffffffffu, t, o);
   return t;
 }
