@@ -157,7 +157,7 @@ def measure_adjoint(n=96, reps=2):
             "cg_iters": {"forward": P.iters[0], "adjoint": P.iters[1]}, "rtol": 1e-10}
 
 
-def measure_batched(n_hex=128, n_tet=128, reps=3):
+def measure_batched(n_hex=128, n_tet=128, reps=3, tune=True):
     """Batched adjoint gradients of 256 ragged problems (n ~ U{8..48}); batched persistent graph vs the
     same problems one at a time through the plain forward/backward pair."""
     import torch
@@ -167,6 +167,9 @@ def measure_batched(n_hex=128, n_tet=128, reps=3):
 
     probs = batch.make_problems(n_hex=n_hex, n_tet=n_tet)
     groups = [batch.Batch([p for p in probs if p["etype"] == 2]), batch.Batch([p for p in probs if p["etype"] == 0])]
+    # the autotuner picks each batch's element kernel (elements per CTA, scatter)
+    tuning = [g.ctx.autotune(op0={"stiffness": 2, "stiff_coef": 1.0, "apply_bc": 1}, op1={"mass": 1, "mass_coef": 1.0},
+                             rhs={"kind": 1, "fn": 0, "coef": 1.0, "apply_bc": 1}) for g in groups] if tune else None
     batch.batch_adjoint(groups)  # builds and replays the graph
     torch.cuda.synchronize()
     ts = []
@@ -207,7 +210,8 @@ def measure_batched(n_hex=128, n_tet=128, reps=3):
             "problems": n_hex + n_tet, "elements": E, "batched_grads_per_s": (n_hex + n_tet) / tb,
             "sequential_grads_per_s": (n_hex + n_tet) / ts_, "speedup": ts_ / tb, "batched_ms": 1e3 * tb,
             "sequential_ms": 1e3 * ts_, "max_cg_iters": iters,
-            "grad_rel_err_vs_plain": err, "rtol": 1e-10, "launch": "one CUDA graph: 2 assembly kernels, "
+            "grad_rel_err_vs_plain": err, "rtol": 1e-10, "tuning": tuning,
+            "launch": "one CUDA graph: 2 assembly kernels, "
             "1 persistent cooperative solver (forward CG, loss, adjoint CG), 2 gradient kernels"}
 
 
@@ -259,6 +263,7 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--cpu-n", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default kernels)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-gradient measurement")
@@ -299,6 +304,8 @@ def main():
     opK = {"stiffness": 2, "stiff_coef": 1.0}
     opM = {"mass": 1, "mass_coef": 1.0}
     rhs = {"kind": 1, "fn": L.FN_SIN3, "coef": 1.0}
+    # autotuner: elements per CTA x scatter strategy, timed on this mesh (setup, untimed)
+    tuning = None if args.no_tune else ctx.autotune(op0=opK, op1=opM, rhs=rhs)
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
 
@@ -422,7 +429,7 @@ def main():
     if rank == 0 and not args.no_adjoint:
         adjoint = measure_adjoint()
     if rank == 0 and not args.no_batched:
-        batched = measure_batched()
+        batched = measure_batched(tune=not args.no_tune)
 
     if rank == 0:
         line = {
@@ -430,7 +437,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded perturbed cube)",
             "config": {"workload": f"q1hex perturbed {n}^3: K(k_e)+M+rhs sin3, fused pass + prune check",
-                       "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned),
+                       "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned), "tuning": tuning,
                        "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
                        "setup_s": setup_s, "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,

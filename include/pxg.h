@@ -113,6 +113,27 @@ typedef struct pxg_rhs_op
 /* pxg_assemble flags */
 #define PXG_ACCUMULATE 1u /* add into vals0/vals1/b instead of overwriting them */
 
+/* Scatter of the element contributions into the CSR values. */
+typedef enum pxg_scatter
+{
+  PXG_SCATTER_REDUCE = 0, /* FP64 reductions in element order (default) */
+  PXG_SCATTER_COLOUR = 1  /* one launch per element colour class: every CSR entry gets at
+                             most one contribution per launch, so the sums are formed in a
+                             fixed order and the matrices are bitwise reproducible */
+} pxg_scatter;
+
+/* Outcome of pxg_autotune: the chosen configuration and every candidate's time. */
+typedef struct pxg_tune_report
+{
+  int threads;  /* threads per block of the element kernel (8 per element for Q1 hexahedra) */
+  int scatter;  /* pxg_scatter */
+  int ncolours; /* colour classes of the colouring (0 if it was not built) */
+  int ncand;
+  int cand_threads[16];
+  int cand_scatter[16];
+  double cand_ms[16]; /* mean time of one pxg_assemble call with the tuned operators */
+} pxg_tune_report;
+
 /* ----------------------------------------------------------------- context */
 pxg_status pxg_create(pxg_ctx ** ctx, int device);
 pxg_status pxg_destroy(pxg_ctx * ctx);
@@ -179,6 +200,21 @@ pxg_status pxg_prune_count(pxg_ctx * ctx, const double * vals, int64_t * pruned,
  * (device memory, one int64) and returns without waiting, so that assembly, the check
  * and the read-back of several steps can overlap. */
 pxg_status pxg_prune_count_device(pxg_ctx * ctx, const double * vals, int64_t * pruned_dev, void * stream);
+
+/* Scatter strategy and threads per block of the element kernels (threads = 0: the
+ * kernel's default).  Valid thread counts: 64, 128, 256 (P1/P2 tetrahedra), 128, 256,
+ * 512 (Q1 hexahedra), 128 (Q2 hexahedra).  PXG_SCATTER_COLOUR builds the element
+ * colouring on the first use (not during a stream capture). */
+pxg_status pxg_set_scatter(pxg_ctx * ctx, int scatter, int threads);
+/* Element colouring of the colour-ordered scatter (built if needed): the number of
+ * colour classes, and optionally the elements in colour order (nelem entries) and the
+ * class offsets (ncolours + 1 entries), host arrays. */
+pxg_status pxg_colouring(pxg_ctx * ctx, int * ncolours, uint32_t * order, int64_t * offsets);
+/* Autotuner: times every (threads, scatter) candidate of this context's element type on
+ * its own mesh with the given operators (outputs into scratch arrays), keeps the fastest
+ * with pxg_set_scatter and reports the candidates.  Call it outside stream capture. */
+pxg_status pxg_autotune(pxg_ctx * ctx, const pxg_lhs_op * op0, const pxg_lhs_op * op1,
+                        const pxg_rhs_op * rhs, pxg_tune_report * report);
 /* Compact: write the pruned CSR (row_ptr[ndof+1], col_idx, vals_out; device
  * pointers, capacity nnz) and its entry count. */
 pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_ptr,

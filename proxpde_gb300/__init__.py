@@ -21,15 +21,15 @@ from __future__ import annotations
 import numpy as np
 
 from . import meshgen
-from ._lib import (FN_CONST, FN_POISSON_EXACT, FN_POISSON_RHS, FN_SIN3, P1TET, P2TET, Q1HEX, Q2HEX, Context,
-                   PxgError, load)
+from ._lib import (FN_CONST, FN_POISSON_EXACT, FN_POISSON_RHS, FN_SIN3, P1TET, P2TET, Q1HEX, Q2HEX,
+                   SCATTER_COLOUR, SCATTER_REDUCE, Context, PxgError, load)
 
 __all__ = [
     "Tetrahedron", "Hexahedron", "Mesh", "buildHyperCube", "FESpace", "BCEss", "side", "Builder",
     "AssemblyStiffness", "AssemblyStiffnessFE", "AssemblyScalarMass", "AssemblyMass", "AssemblyRhsAnalytic",
     "AssemblyS2SProjection", "AssemblyProjection", "interpolateAnalyticFunction", "Context", "PxgError",
     "FN_CONST", "FN_SIN3", "FN_POISSON_RHS", "FN_POISSON_EXACT", "P1TET", "P2TET", "Q1HEX", "Q2HEX", "meshgen",
-    "load",
+    "load", "SCATTER_REDUCE", "SCATTER_COLOUR",
 ]
 
 

@@ -28,7 +28,8 @@ EXPORTS = [
     "pxg_create", "pxg_destroy", "pxg_last_error", "pxg_status_string", "pxg_version",
     "pxg_set_mesh", "pxg_set_coords", "pxg_build_dofmap", "pxg_set_dofmap", "pxg_get_dofmap",
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
-    "pxg_assemble", "pxg_prune_count", "pxg_prune_count_device", "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
+    "pxg_assemble", "pxg_prune_count", "pxg_prune_count_device", "pxg_set_scatter", "pxg_colouring", "pxg_autotune",
+    "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
     "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
 ]
@@ -59,6 +60,21 @@ class RhsOp(C.Structure):
         ("apply_bc", C.c_int32),
     ]
 
+
+class TuneReport(C.Structure):
+    _fields_ = [
+        ("threads", C.c_int),
+        ("scatter", C.c_int),
+        ("ncolours", C.c_int),
+        ("ncand", C.c_int),
+        ("cand_threads", C.c_int * 16),
+        ("cand_scatter", C.c_int * 16),
+        ("cand_ms", C.c_double * 16),
+    ]
+
+
+SCATTER_REDUCE, SCATTER_COLOUR = 0, 1
+SCATTER_NAMES = {SCATTER_REDUCE: "reduce", SCATTER_COLOUR: "colour"}
 
 _lib = None
 
@@ -92,6 +108,9 @@ def load(path: str = LIB_PATH):
                          C.c_int),
         "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
         "pxg_prune_count_device": ([vp, vp, vp, vp], C.c_int),
+        "pxg_set_scatter": ([vp, C.c_int, C.c_int], C.c_int),
+        "pxg_colouring": ([vp, C.POINTER(C.c_int), vp, vp], C.c_int),
+        "pxg_autotune": ([vp, C.POINTER(LhsOp), C.POINTER(LhsOp), C.POINTER(RhsOp), C.POINTER(TuneReport)], C.c_int),
         "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_interpolate": ([vp, C.c_int, C.c_double, vp, vp], C.c_int),
         "pxg_prune_csr_noalloc": ([vp, vp, vp, i64, vp, vp, vp, i64p, vp], C.c_int),
@@ -222,21 +241,24 @@ class Context:
                     "set_bc")
 
     # --- assembly
+    @staticmethod
+    def _lhs(o):
+        if o is None:
+            return None
+        return C.pointer(LhsOp(int(o.get("stiffness", 0)), float(o.get("stiff_coef", 1.0)), int(o.get("mass", 0)),
+                               float(o.get("mass_coef", 1.0)), int(o.get("apply_bc", 0))))
+
+    @staticmethod
+    def _rhs(rhs):
+        if rhs is None:
+            return None
+        return C.pointer(RhsOp(int(rhs.get("kind", 0)), int(rhs.get("fn", 0)), float(rhs.get("coef", 1.0)),
+                               _ptr(rhs.get("field")), int(rhs.get("apply_bc", 0))))
+
     def assemble(self, op0=None, vals0=None, op1=None, vals1=None, rhs=None, b=None, accumulate=False,
                  stream=None):
-        def lhs(o):
-            if o is None:
-                return None
-            return C.pointer(LhsOp(int(o.get("stiffness", 0)), float(o.get("stiff_coef", 1.0)),
-                                   int(o.get("mass", 0)), float(o.get("mass_coef", 1.0)),
-                                   int(o.get("apply_bc", 0))))
-
-        r = None
-        if rhs is not None:
-            r = C.pointer(RhsOp(int(rhs.get("kind", 0)), int(rhs.get("fn", 0)), float(rhs.get("coef", 1.0)),
-                                _ptr(rhs.get("field")), int(rhs.get("apply_bc", 0))))
-        self._check(self.L.pxg_assemble(self.h, lhs(op0), _ptr(vals0), lhs(op1), _ptr(vals1), r, _ptr(b),
-                                        ACCUMULATE if accumulate else 0, stream), "assemble")
+        self._check(self.L.pxg_assemble(self.h, self._lhs(op0), _ptr(vals0), self._lhs(op1), _ptr(vals1),
+                                        self._rhs(rhs), _ptr(b), ACCUMULATE if accumulate else 0, stream), "assemble")
 
     def prune_count(self, vals, stream=None):
         n = C.c_int64()
@@ -247,6 +269,31 @@ class Context:
         """Asynchronous prune count into `out` (a one-element int64 device tensor)."""
         assert str(out.dtype) == "torch.int64" and out.is_cuda and out.numel() >= 1
         self._check(self.L.pxg_prune_count_device(self.h, _ptr(vals), _ptr(out), stream), "prune_count_device")
+
+    # --- scatter strategy and autotuning
+    def set_scatter(self, scatter, threads=0):
+        self._check(self.L.pxg_set_scatter(self.h, int(scatter), int(threads)), "set_scatter")
+
+    def colouring(self, with_order=False):
+        """(number of colour classes, element order or None, class offsets or None)"""
+        n = C.c_int()
+        self._check(self.L.pxg_colouring(self.h, C.byref(n), None, None), "colouring")
+        if not with_order:
+            return n.value, None, None
+        order = np.empty(self.nelem, dtype=np.uint32)
+        offs = np.empty(n.value + 1, dtype=np.int64)
+        self._check(self.L.pxg_colouring(self.h, C.byref(n), order.ctypes.data, offs.ctypes.data), "colouring")
+        return n.value, order, offs
+
+    def autotune(self, op0=None, op1=None, rhs=None):
+        """Time every (threads, scatter) candidate on this mesh, keep the fastest; returns
+        dict(threads, scatter, ncolours, candidates=[(threads, scatter, ms)])."""
+        rep = TuneReport()
+        self._check(self.L.pxg_autotune(self.h, self._lhs(op0), self._lhs(op1), self._rhs(rhs), C.byref(rep)),
+                    "autotune")
+        cands = [(rep.cand_threads[i], SCATTER_NAMES[rep.cand_scatter[i]], rep.cand_ms[i]) for i in range(rep.ncand)]
+        return {"threads": rep.threads, "scatter": SCATTER_NAMES[rep.scatter], "ncolours": rep.ncolours,
+                "candidates": cands}
 
     def close_matrix(self, vals, rp, ci, vout, stream=None):
         n = C.c_int64()

@@ -183,6 +183,12 @@ pxg_status pxg_set_mesh(pxg_ctx * c, int etype, double const * xyz, int64_t nnod
   c->rank.reset();
   c->kE.reset();
   c->hasCoef = false;
+  c->colour.perm.reset();
+  c->colour.start.clear();
+  c->colour.ncol = 0;
+  c->colour.built = false;
+  c->scatter = PXG_SCATTER_REDUCE;
+  c->threads = 0;
   c->bcMask.reset();
   c->bcVal.reset();
   c->nbc = 0;

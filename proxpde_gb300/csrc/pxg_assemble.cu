@@ -328,14 +328,15 @@ __device__ __forceinline__ void gram(double const (&A)[3][3], double s, double *
 
 __device__ __forceinline__ void red(double * p, double v) { atomicAdd(p, v); }
 
-template <int T>
-__global__ void __launch_bounds__(128) kAssemble(AsmArgs a)
+template <int T, int NT>
+__global__ void __launch_bounds__(NT) kAssemble(AsmArgs a)
 {
   constexpr int NV = Elem<T>::NV, N = Elem<T>::N, NQ = Elem<T>::NQ;
   constexpr bool HEX = Elem<T>::hex;
-  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= a.nelem)
+  int64_t const i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i0 >= a.nelem)
     return;
+  int64_t const e = elemOf(a, i0);
 
   double X[NV][3];
 #pragma unroll
@@ -769,11 +770,35 @@ using namespace pxg;
 
 namespace
 {
+// Threads per block: 64, 128 or 256 for the tetrahedra (autotuner candidates), 128
+// for the hexahedra of the generic kernel.
 template <int T>
-void launchAssemble(AsmArgs const & a, cudaStream_t s)
+void launchAssemble(AsmArgs const & a, cudaStream_t s, int threads)
 {
-  unsigned const blocks = (unsigned)((a.nelem + 127) / 128);
-  kAssemble<T><<<blocks, 128, 0, s>>>(a);
+  auto go = [&](auto kern, int nt) {
+    unsigned const blocks = (unsigned)((a.nelem + nt - 1) / nt);
+    kern<<<blocks, nt, 0, s>>>(a);
+  };
+  if constexpr (T == P1TET || T == P2TET)
+  {
+    if (threads == 64)
+      return go(kAssemble<T, 64>, 64);
+    if (threads == 256)
+      return go(kAssemble<T, 256>, 256);
+  }
+  go(kAssemble<T, 128>, 128);
+}
+
+// Candidate thread counts of the autotuner for an element type (0-terminated)
+void threadCandidates(pxg_ctx const * c, int (&out)[4])
+{
+  out[0] = out[1] = out[2] = out[3] = 0;
+  if (c->etype == P1TET || c->etype == P2TET)
+    out[0] = 64, out[1] = 128, out[2] = 256;
+  else if (c->etype == Q1HEX && !c->q1Generic && !c->q1Thread)
+    out[0] = 128, out[1] = 256, out[2] = 512;
+  else
+    out[0] = 128;
 }
 } // namespace
 
@@ -847,26 +872,175 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     if (b)
       PXG_CUDA(c, cudaMemsetAsync(b, 0, (size_t)c->ndof * 8, s));
   }
-  switch (c->etype)
+  auto launch = [&](AsmArgs const & la) {
+    switch (c->etype)
+    {
+    case P1TET:
+      launchAssemble<P1TET>(la, s, c->threads);
+      break;
+    case P2TET:
+      launchAssemble<P2TET>(la, s, c->threads);
+      break;
+    case Q1HEX:
+      if (c->q1Generic)
+        launchAssemble<Q1HEX>(la, s, c->threads);
+      else
+        launchAssembleQ1(la, s, c->q1Fp64, c->q1Thread, c->threads);
+      break;
+    case Q2HEX:
+      launchAssemble<Q2HEX>(la, s, c->threads);
+      break;
+    }
+  };
+  if (c->scatter == PXG_SCATTER_COLOUR)
   {
-  case P1TET:
-    launchAssemble<P1TET>(a, s);
-    break;
-  case P2TET:
-    launchAssemble<P2TET>(a, s);
-    break;
-  case Q1HEX:
-    if (c->q1Generic)
-      launchAssemble<Q1HEX>(a, s);
-    else
-      launchAssembleQ1(a, s, c->q1Fp64, c->q1Thread);
-    break;
-  case Q2HEX:
-    launchAssemble<Q2HEX>(a, s);
-    break;
+    if (!c->colour.built)
+    {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      PXG_CUDA(c, cudaStreamIsCapturing(s, &cs));
+      if (cs != cudaStreamCaptureStatusNone)
+        return fail(c, PXG_ERR_INVALID_ARG, "the colour-ordered scatter needs its colouring before a stream capture");
+      if ((st = buildColouring(c)) != PXG_OK)
+        return st;
+    }
+    // one launch per colour class, in colour order
+    for (int k = 0; k < c->colour.ncol; ++k)
+    {
+      AsmArgs la = a;
+      la.perm = c->colour.perm.p;
+      la.permBase = c->colour.start[k];
+      la.nelem = c->colour.start[k + 1] - c->colour.start[k];
+      if (la.nelem > 0)
+        launch(la);
+    }
   }
+  else
+    launch(a);
   PXG_CUDA(c, cudaGetLastError());
   return PXG_OK;
+}
+
+pxg_status pxg_set_scatter(pxg_ctx * c, int scatter, int threads)
+{
+  if (!c || (scatter != PXG_SCATTER_REDUCE && scatter != PXG_SCATTER_COLOUR))
+    return PXG_ERR_INVALID_ARG;
+  if (c->etype < 0)
+    return fail(c, PXG_ERR_INVALID_ARG, "set the mesh first");
+  if (threads)
+  {
+    int cand[4];
+    threadCandidates(c, cand);
+    bool ok = false;
+    for (int t : cand)
+      ok = ok || (t && t == threads);
+    if (!ok)
+      return fail(c, PXG_ERR_INVALID_ARG, "%d threads per block is not a variant of this element kernel", threads);
+  }
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  if (scatter == PXG_SCATTER_COLOUR && (st = buildColouring(c)) != PXG_OK)
+    return st;
+  c->scatter = scatter;
+  c->threads = threads;
+  return PXG_OK;
+}
+
+pxg_status pxg_colouring(pxg_ctx * c, int * ncolours, uint32_t * order, int64_t * offsets)
+{
+  if (!c || !ncolours)
+    return PXG_ERR_INVALID_ARG;
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  if ((st = buildColouring(c)) != PXG_OK)
+    return st;
+  *ncolours = c->colour.ncol;
+  if (order)
+    PXG_CUDA(c, cudaMemcpy(order, c->colour.perm.p, (size_t)c->nelem * 4, cudaMemcpyDeviceToHost));
+  if (offsets)
+    for (int k = 0; k <= c->colour.ncol; ++k)
+      offsets[k] = c->colour.start[k];
+  return PXG_OK;
+}
+
+pxg_status pxg_autotune(pxg_ctx * c, pxg_lhs_op const * op0, pxg_lhs_op const * op1, pxg_rhs_op const * rhs,
+                        pxg_tune_report * rep)
+{
+  if (!c || !rep)
+    return PXG_ERR_INVALID_ARG;
+  if (!c->rowPtr.p)
+    return fail(c, PXG_ERR_INVALID_ARG, "build the pattern first");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  // scratch outputs
+  DevBuf<double> v0, v1, bb;
+  if (op0)
+    PXG_CUDA(c, v0.alloc(c->nnz));
+  if (op1)
+    PXG_CUDA(c, v1.alloc(c->nnz));
+  if (rhs && rhs->kind)
+    PXG_CUDA(c, bb.alloc(c->ndof));
+  int cand[4];
+  threadCandidates(c, cand);
+  bool const colourOk = buildColouring(c) == PXG_OK;
+  int const keepScatter = c->scatter, keepThreads = c->threads;
+  cudaStream_t s = nullptr;
+  PXG_CUDA(c, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PXG_CUDA(c, cudaEventCreate(&e0));
+  PXG_CUDA(c, cudaEventCreate(&e1));
+  *rep = pxg_tune_report{};
+  rep->ncolours = colourOk ? c->colour.ncol : 0;
+  double best = 1e300;
+  int bestT = keepThreads, bestS = keepScatter;
+  st = PXG_OK;
+  for (int sc = 0; sc < 2 && st == PXG_OK; ++sc)
+  {
+    if (sc == PXG_SCATTER_COLOUR && !colourOk)
+      continue;
+    for (int t : cand)
+    {
+      if (!t || rep->ncand >= 16 || st != PXG_OK)
+        break;
+      c->scatter = sc;
+      c->threads = t;
+      auto run = [&] { return pxg_assemble(c, op0, v0.p, op1, v1.p, rhs, bb.p, 0u, s); };
+      if ((st = run()) != PXG_OK) // warm-up
+        break;
+      constexpr int kReps = 3;
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < kReps && st == PXG_OK; ++r)
+        st = run();
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess)
+        st = cudaFail(c, cudaGetLastError(), "autotune");
+      if (st != PXG_OK)
+        break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      double const per = ms / kReps;
+      rep->cand_threads[rep->ncand] = t;
+      rep->cand_scatter[rep->ncand] = sc;
+      rep->cand_ms[rep->ncand] = per;
+      ++rep->ncand;
+      if (per < best)
+      {
+        best = per;
+        bestT = t;
+        bestS = sc;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  c->scatter = st == PXG_OK ? bestS : keepScatter;
+  c->threads = st == PXG_OK ? bestT : keepThreads;
+  rep->threads = c->threads;
+  rep->scatter = c->scatter;
+  return st;
 }
 
 pxg_status pxg_prune_count(pxg_ctx * c, double const * vals, int64_t * pruned, void * stream)

@@ -896,6 +896,8 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
       key.ctx[i] = ctxs[i];
       key.ut[i] = u_targets[i];
       key.grad[i] = grads[i];
+      key.scatter[i] = ctxs[i]->scatter;
+      key.threads[i] = ctxs[i]->threads;
     }
     key.rhs = *rhs;
     key.rtol = rtol;

@@ -233,11 +233,14 @@ struct GraphKey
   pxg_rhs_op rhs{};
   double rtol = 0.;
   int maxIter = 0;
+  int scatter[2] = {0, 0}, threads[2] = {0, 0}; // the element kernels captured in the graph
   bool operator==(GraphKey const & o) const
   {
     return nctx == o.nctx && ctx[0] == o.ctx[0] && ctx[1] == o.ctx[1] && ut[0] == o.ut[0] && ut[1] == o.ut[1] &&
            grad[0] == o.grad[0] && grad[1] == o.grad[1] && rhs.kind == o.rhs.kind && rhs.fn == o.rhs.fn &&
-           rhs.coef == o.rhs.coef && rhs.field == o.rhs.field && rtol == o.rtol && maxIter == o.maxIter;
+           rhs.coef == o.rhs.coef && rhs.field == o.rhs.field && rtol == o.rtol && maxIter == o.maxIter &&
+           scatter[0] == o.scatter[0] && scatter[1] == o.scatter[1] && threads[0] == o.threads[0] &&
+           threads[1] == o.threads[1];
   }
 };
 
@@ -293,6 +296,19 @@ struct pxg_ctx
   double bcDiag = 1.0;
   // small device scratch (counters, flags)
   pxg::DevBuf<unsigned long long> counter;
+  // scatter strategy and elements per CTA of the element kernels (pxg_set_scatter,
+  // pxg_autotune); threads = 0 is the kernel's default
+  int scatter = 0; // PXG_SCATTER_REDUCE or PXG_SCATTER_COLOUR
+  int threads = 0;
+  // element colouring of the colour-ordered scatter: elements sorted by colour,
+  // start[k] .. start[k + 1] the k-th colour class
+  struct ColourState
+  {
+    int ncol = 0;
+    std::vector<int64_t> start;
+    pxg::DevBuf<uint32_t> perm;
+    bool built = false;
+  } colour;
   // Q1 hexahedra use the tensor-product kernel in double-float arithmetic; in the
   // environment PXG_Q1_FP64=1 selects its FP64 variant and PXG_Q1_GENERIC=1 the
   // generic kernel (both kept for cross-checks)
@@ -332,9 +348,20 @@ struct AsmArgs
   double rc;
   double const * field;
   double * b;
+  // colour-ordered scatter: the launch covers elements perm[permBase .. permBase + nelem)
+  uint32_t const * perm;
+  int64_t permBase;
 };
 
-void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread);
+// element id of the launch's i-th element
+__device__ __forceinline__ int64_t elemOf(AsmArgs const & a, int64_t i)
+{
+  return a.perm ? (int64_t)a.perm[a.permBase + i] : i;
+}
+
+void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread, int threads);
+// element colouring (pxg_colour.cu); built once per mesh
+pxg_status buildColouring(pxg_ctx * c);
 
 struct AdjArgs
 {

@@ -365,9 +365,10 @@ template <typename T>
 __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
 {
   using namespace q1;
-  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= a.nelem)
+  int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= a.nelem)
     return;
+  int64_t const e = elemOf(a, i);
 
   double X[8][3];
   uint32_t dof[8];
@@ -579,11 +580,12 @@ namespace q1g
 {
 using namespace q1;
 
-// Threads per block.  The phases end at block barriers: the eight warps of a block
-// then run the same phase, and the SM's instruction cache holds the code of at most
-// four phases (one per resident block).  Measured at 128^3 (ms per launch): 128
-// threads with warp-level syncs 3.11, 128 / 256 / 512 / 1024 threads with block
-// barriers 3.03 / 2.77 / 3.09 / 3.40; 256 threads at 80 registers 2.99.
+// Threads per block (default; 128 and 512 are the other candidates of the autotuner).
+// The phases end at block barriers: the warps of a block then run the same phase, and
+// the SM's instruction cache holds the code of a few phases only (one per resident
+// block).  Measured at 128^3 (ms per launch): 128 threads with warp-level syncs 3.11,
+// 128 / 256 / 512 / 1024 threads with block barriers 3.03 / 2.77 / 3.09 / 3.40; 256
+// threads at 80 registers 2.99.
 constexpr int kThreads = 256;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kAlpha01 = 0.5 * (AA + BB), kBeta0 = 0.5 * (AA - BB);
@@ -602,7 +604,11 @@ struct __align__(16) ElemShared
   uint16_t rank[64]; // scatter ranks of the element's 8 x 8 entries
   uint32_t pad[16];  // slot stride 1088 B: the four groups of a warp start 16 banks apart
 };
-constexpr size_t kSmemBytes = (kThreads / 8) * sizeof(ElemShared<dfl>) + 36 * sizeof(uint4);
+template <int NT>
+constexpr size_t smemBytes()
+{
+  return (NT / 8) * sizeof(ElemShared<dfl>) + 36 * sizeof(uint4);
+}
 
 __device__ __forceinline__ dfl shx(dfl v, int m)
 {
@@ -752,12 +758,12 @@ __device__ __forceinline__ T pick3(T const (&v)[3], int d)
   return d == 0 ? v[0] : (d == 1 ? v[1] : v[2]);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads, 4) kAssembleQ1Group(AsmArgs a)
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
 {
-  extern __shared__ uint4 dynShared[]; // ElemShared<T>[kThreads / 8], then the 36 pair descriptors
+  extern __shared__ uint4 dynShared[]; // ElemShared<T>[NT / 8], then the 36 pair descriptors
   ElemShared<T> * shAll = reinterpret_cast<ElemShared<T> *>(dynShared);
-  uint4 * sDesc = reinterpret_cast<uint4 *>(shAll + kThreads / 8);
+  uint4 * sDesc = reinterpret_cast<uint4 *>(shAll + NT / 8);
   if (threadIdx.x < 36)
     sDesc[threadIdx.x] = pairDesc(threadIdx.x);
   __syncthreads();
@@ -765,9 +771,9 @@ __global__ void __launch_bounds__(kThreads, 4) kAssembleQ1Group(AsmArgs a)
   int const l = threadIdx.x & 7;
   int const g0 = threadIdx.x & 24; // first lane of the group in the warp
   ElemShared<T> & sh = shAll[threadIdx.x >> 3];
-  int64_t const eg = ((int64_t)blockIdx.x * kThreads + threadIdx.x) >> 3;
+  int64_t const eg = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 3;
   bool const live = eg < a.nelem;
-  int64_t const e = live ? eg : a.nelem - 1; // a tail group recomputes the last element, writes nothing
+  int64_t const e = elemOf(a, live ? eg : a.nelem - 1); // a tail group recomputes the last element, writes nothing
   int const bx = l & 1, by = (l >> 1) & 1, bz = l >> 2;
   bool const lhs = a.op[0].on || a.op[1].on;
 
@@ -1036,7 +1042,7 @@ __global__ void __launch_bounds__(kThreads, 4) kAssembleQ1Group(AsmArgs a)
 }
 } // namespace q1g
 
-void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread)
+void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread, int threads)
 {
   if (perThread)
   {
@@ -1047,11 +1053,21 @@ void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThre
       kAssembleQ1<dfl><<<blocks, 128, 0, s>>>(a);
     return;
   }
-  unsigned const blocks = (unsigned)((a.nelem * 8 + q1g::kThreads - 1) / q1g::kThreads);
+  auto go = [&](auto kern, int nt, size_t smem) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    unsigned const blocks = (unsigned)((a.nelem * 8 + nt - 1) / nt);
+    kern<<<blocks, nt, smem, s>>>(a);
+  };
+  int const nt = threads ? threads : q1g::kThreads;
   if (fp64)
-    q1g::kAssembleQ1Group<double><<<blocks, q1g::kThreads, q1g::kSmemBytes, s>>>(a);
+    go(q1g::kAssembleQ1Group<double, q1g::kThreads>, q1g::kThreads, q1g::smemBytes<q1g::kThreads>());
+  else if (nt == 128)
+    go(q1g::kAssembleQ1Group<dfl, 128>, 128, q1g::smemBytes<128>());
+  else if (nt == 512)
+    go(q1g::kAssembleQ1Group<dfl, 512>, 512, q1g::smemBytes<512>());
   else
-    q1g::kAssembleQ1Group<dfl><<<blocks, q1g::kThreads, q1g::kSmemBytes, s>>>(a);
+    go(q1g::kAssembleQ1Group<dfl, 256>, 256, q1g::smemBytes<256>());
 }
 
 // Adjoint gradient g_e = -(C u)_e^T K_e (C lambda)_e, K_e = k_e K0_e (Q1, 2x2x2 rule):

@@ -22,8 +22,9 @@ def problem(gen, n, alpha=0.0, seed=1, sigma=None):
     return xyz, conn, k
 
 
-def gpu_assemble(t, xyz, conn, ops, rhs=None, k=None, bc=None, device=0, field=None):
-    """Run the engine through the C ABI. ops: list of up to two lhs op dicts.
+def gpu_assemble(t, xyz, conn, ops, rhs=None, k=None, bc=None, device=0, field=None, scatter=None, threads=0):
+    """Run the engine through the C ABI. ops: list of up to two lhs op dicts; scatter /
+    threads select the scatter strategy and the block size (None: defaults).
     Returns dict(em, ndof, pattern, mats=[(rp, col, val)], b)."""
     import torch
 
@@ -33,6 +34,8 @@ def gpu_assemble(t, xyz, conn, ops, rhs=None, k=None, bc=None, device=0, field=N
     ctx.set_mesh(t, xyz, conn)
     ndof = ctx.build_dofmap()
     nnz = ctx.build_pattern()
+    if scatter is not None:
+        ctx.set_scatter(scatter, threads)
     if k is not None:
         ctx.set_coef(np.ascontiguousarray(k))
     if bc is not None:
