@@ -69,6 +69,64 @@ __device__ __forceinline__ dfl fma(dfl a, dfl b, dfl c) { return a * b + c; }
 __device__ __forceinline__ dfl fabs(dfl a) { return a.h < 0.f ? -a : a; }
 __device__ __forceinline__ bool operator<(dfl a, float b) { return a.h < b; }
 
+// Fused expressions: the products are formed exactly with FMAs (TwoProd), the high
+// parts summed with TwoSum, and everything of order 2^-24 (product errors, cross terms
+// a.h * b.l, the low parts) gathered in one float before a single renormalisation.
+// Same accuracy class as the chained operations (relative ~2^-47 of the sum of the
+// magnitudes), fewer instructions: a*b + c*d 19 instead of 25, the 3-term dot product
+// 31 instead of 43 (the compensated dot product of Ogita, Rump and Oishi, "Accurate
+// sum and dot product", SIAM J. Sci. Comput. 26(6), 2005, on double-word inputs).
+__device__ __forceinline__ dfl dot2(dfl a, dfl b, dfl c, dfl d)
+{
+  float const p1 = __fmul_rn(a.h, b.h), p2 = __fmul_rn(c.h, d.h);
+  float lo = __fadd_rn(__fmaf_rn(a.h, b.h, -p1), __fmaf_rn(c.h, d.h, -p2));
+  dfl const s = dflTwoSum(p1, p2);
+  lo = __fadd_rn(lo, s.l);
+  lo = __fmaf_rn(a.h, b.l, lo);
+  lo = __fmaf_rn(a.l, b.h, lo);
+  lo = __fmaf_rn(c.h, d.l, lo);
+  lo = __fmaf_rn(c.l, d.h, lo);
+  return dflFastTwoSum(s.h, lo);
+}
+__device__ __forceinline__ dfl dot3(dfl a, dfl b, dfl c, dfl d, dfl e, dfl f)
+{
+  float const p1 = __fmul_rn(a.h, b.h), p2 = __fmul_rn(c.h, d.h), p3 = __fmul_rn(e.h, f.h);
+  float lo = __fadd_rn(__fadd_rn(__fmaf_rn(a.h, b.h, -p1), __fmaf_rn(c.h, d.h, -p2)), __fmaf_rn(e.h, f.h, -p3));
+  dfl const s1 = dflTwoSum(p1, p2);
+  dfl const s2 = dflTwoSum(s1.h, p3);
+  lo = __fadd_rn(lo, __fadd_rn(s1.l, s2.l));
+  lo = __fmaf_rn(a.h, b.l, lo);
+  lo = __fmaf_rn(a.l, b.h, lo);
+  lo = __fmaf_rn(c.h, d.l, lo);
+  lo = __fmaf_rn(c.l, d.h, lo);
+  lo = __fmaf_rn(e.h, f.l, lo);
+  lo = __fmaf_rn(e.l, f.h, lo);
+  return dflFastTwoSum(s2.h, lo);
+}
+__device__ __forceinline__ double dot2(double a, double b, double c, double d) { return a * b + c * d; }
+__device__ __forceinline__ double dot3(double a, double b, double c, double d, double e, double f)
+{
+  return a * b + c * d + e * f;
+}
+
+// Running sum of double-float terms: TwoSum on the high parts, the errors and the low
+// parts in one float (8 instructions a term instead of 11), one renormalisation at the end.
+struct DflSum
+{
+  float s, c;
+};
+__device__ __forceinline__ DflSum sumStart(dfl t) { return DflSum{t.h, t.l}; }
+__device__ __forceinline__ void sumAdd(DflSum & a, dfl t)
+{
+  dfl const s = dflTwoSum(a.s, t.h);
+  a.s = s.h;
+  a.c = __fadd_rn(a.c, __fadd_rn(s.l, t.l));
+}
+__device__ __forceinline__ dfl sumEnd(DflSum a) { return dflFastTwoSum(a.s, a.c); }
+__device__ __forceinline__ double sumStart(double t) { return t; }
+__device__ __forceinline__ void sumAdd(double & a, double t) { a += t; }
+__device__ __forceinline__ double sumEnd(double a) { return a; }
+
 // 1/a: float reciprocal refined by one Newton step in double-float
 __device__ __forceinline__ dfl rcp(dfl a)
 {

@@ -121,7 +121,7 @@ __device__ __forceinline__ dfl sinpiNear(dfl so, dfl co, double o, dfl d)
     dfl const es = dfl{hs, 0.f} - u2 * cst<dfl>(1.0 / 6.0); // sin u = u (1 + es)
     dfl const c = (cst<dfl>(1.0) - dfl{0.5f * u2.h, 0.5f * u2.l}) + dfl{hc, 0.f};
     dfl const s = u + u * es;
-    return so * c + co * s;
+    return dot2(so, c, co, s);
   }
   return sinpiFar(o, d);
 }
@@ -641,7 +641,7 @@ __device__ __forceinline__ double scl(double v, double s) { return v * s; }
 template <typename T>
 __device__ __forceinline__ T lerp2(T v, int m)
 {
-  return cst<T>(A) * v + cst<T>(B) * shx(v, m);
+  return dot2(cst<T>(A), v, cst<T>(B), shx(v, m));
 }
 
 // sin(pi o), cos(pi o): o = k/2 + r with |r| <= 1/4 (exact in FP64; adding 1.5 * 2^52
@@ -811,52 +811,52 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
     {
       T const p = shx(Y[r], 1);
       Dx[r] = halfSgn(Y[r] - p, bx);
-      Lx[r] = cst<T>(A) * Y[r] + cst<T>(B) * p;
+      Lx[r] = dot2(cst<T>(A), Y[r], cst<T>(B), p);
     }
     T DxLy[3], LxDy[3], LxLy[3];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
     {
       T const pd = shx(Dx[r], 2), pl = shx(Lx[r], 2);
-      DxLy[r] = cst<T>(A) * Dx[r] + cst<T>(B) * pd;
+      DxLy[r] = dot2(cst<T>(A), Dx[r], cst<T>(B), pd);
       LxDy[r] = halfSgn(Lx[r] - pl, by);
-      LxLy[r] = cst<T>(A) * Lx[r] + cst<T>(B) * pl;
+      LxLy[r] = dot2(cst<T>(A), Lx[r], cst<T>(B), pl);
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r)
     {
       T const p1 = shx(DxLy[r], 4), p2 = shx(LxDy[r], 4), p3 = shx(LxLy[r], 4);
-      J[r][0] = cst<T>(A) * DxLy[r] + cst<T>(B) * p1;
-      J[r][1] = cst<T>(A) * LxDy[r] + cst<T>(B) * p2;
+      J[r][0] = dot2(cst<T>(A), DxLy[r], cst<T>(B), p1);
+      J[r][1] = dot2(cst<T>(A), LxDy[r], cst<T>(B), p2);
       J[r][2] = halfSgn(LxLy[r] - p3, bz);
     }
   }
   T adet, off[3];
   {
     T C[3][3]; // adj(J)
-    C[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-    C[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-    C[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-    C[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-    C[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
-    C[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
-    C[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-    C[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
-    C[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-    T const det = J[0][0] * C[0][0] + J[0][1] * C[1][0] + J[0][2] * C[2][0];
+    C[0][0] = dot2(J[1][1], J[2][2], -J[1][2], J[2][1]);
+    C[0][1] = dot2(J[0][2], J[2][1], -J[0][1], J[2][2]);
+    C[0][2] = dot2(J[0][1], J[1][2], -J[0][2], J[1][1]);
+    C[1][0] = dot2(J[1][2], J[2][0], -J[1][0], J[2][2]);
+    C[1][1] = dot2(J[0][0], J[2][2], -J[0][2], J[2][0]);
+    C[1][2] = dot2(J[0][2], J[1][0], -J[0][0], J[1][2]);
+    C[2][0] = dot2(J[1][0], J[2][1], -J[1][1], J[2][0]);
+    C[2][1] = dot2(J[0][1], J[2][0], -J[0][0], J[2][1]);
+    C[2][2] = dot2(J[0][0], J[1][1], -J[0][1], J[1][0]);
+    T const det = dot3(J[0][0], C[0][0], J[0][1], C[1][0], J[0][2], C[2][0]);
     adet = fabs(det);
     T const s = cst<T>(0.25) * rcp(adet);
-    sh.u.G[0][l] = s * (C[0][0] * C[0][0] + C[0][1] * C[0][1] + C[0][2] * C[0][2]);
-    sh.u.G[1][l] = s * (C[1][0] * C[1][0] + C[1][1] * C[1][1] + C[1][2] * C[1][2]);
-    sh.u.G[2][l] = s * (C[2][0] * C[2][0] + C[2][1] * C[2][1] + C[2][2] * C[2][2]);
-    sh.u.G[3][l] = s * (C[0][0] * C[1][0] + C[0][1] * C[1][1] + C[0][2] * C[1][2]);
-    sh.u.G[4][l] = s * (C[0][0] * C[2][0] + C[0][1] * C[2][1] + C[0][2] * C[2][2]);
-    sh.u.G[5][l] = s * (C[1][0] * C[2][0] + C[1][1] * C[2][1] + C[1][2] * C[2][2]);
+    sh.u.G[0][l] = s * dot3(C[0][0], C[0][0], C[0][1], C[0][1], C[0][2], C[0][2]);
+    sh.u.G[1][l] = s * dot3(C[1][0], C[1][0], C[1][1], C[1][1], C[1][2], C[1][2]);
+    sh.u.G[2][l] = s * dot3(C[2][0], C[2][0], C[2][1], C[2][1], C[2][2], C[2][2]);
+    sh.u.G[3][l] = s * dot3(C[0][0], C[1][0], C[0][1], C[1][1], C[0][2], C[1][2]);
+    sh.u.G[4][l] = s * dot3(C[0][0], C[2][0], C[0][1], C[2][1], C[0][2], C[2][2]);
+    sh.u.G[5][l] = s * dot3(C[1][0], C[2][0], C[1][1], C[2][1], C[1][2], C[2][2]);
     sh.u.G[6][l] = adet;
     T const xq = negIf(cst<T>(g), !bx), yq = negIf(cst<T>(g), !by), zq = negIf(cst<T>(g), !bz);
 #pragma unroll
     for (int r = 0; r < 3; ++r)
-      off[r] = J[r][0] * xq + J[r][1] * yq + J[r][2] * zq;
+      off[r] = dot3(J[r][0], xq, J[r][1], yq, J[r][2], zq);
   }
 
   // ---- D. load vector (and the Dirichlet rows' h, once per operator with bc)
@@ -948,8 +948,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
 #pragma unroll
       for (int qv = 0; qv < 2; ++qv)
       {
-        P0[qw][qv] = a0 * F[qw][qv][0] + a1 * F[qw][qv][1];
-        P1[qw][qv] = cst<T>(B) * F[qw][qv][0] + cst<T>(A) * F[qw][qv][1];
+        P0[qw][qv] = dot2(a0, F[qw][qv][0], a1, F[qw][qv][1]);
+        P1[qw][qv] = dot2(cst<T>(B), F[qw][qv][0], cst<T>(A), F[qw][qv][1]);
       }
     // row r along v: classes W_r (sum jobs, r < 3) or l_(r & 1) of P0 / P1 (U jobs)
     constexpr double kS0[4] = {AA, BB, AB, 0.}, kS1[4] = {BB, AA, AB, 0.};
@@ -964,7 +964,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       {
         T const s0 = (r >= 2 && isU) ? P1[qw][0] : P0[qw][0];
         T const s1 = (r >= 2 && isU) ? P1[qw][1] : P0[qw][1];
-        R[qw] = x0 * s0 + x1 * s1;
+        R[qw] = dot2(x0, s0, x1, s1);
       }
       // classes along w
       T const sum = R[0] + R[1], dif = R[0] - R[1];
@@ -1000,22 +1000,23 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
     T kv = cst<T>(0.0), mv = cst<T>(0.0);
     if (needK)
     {
-      kv = negIf(tb[d.y & 0xffu], neg & 1u);
-      kv = kv + negIf(tb[(d.y >> 8) & 0xffu], (neg >> 1) & 1u);
-      kv = kv + negIf(tb[(d.y >> 16) & 0xffu], (neg >> 2) & 1u);
-      kv = kv + negIf(tb[d.y >> 24], (neg >> 3) & 1u);
-      kv = kv + negIf(tb[d.z & 0xffu], (neg >> 4) & 1u);
-      kv = kv + negIf(tb[(d.z >> 8) & 0xffu], (neg >> 5) & 1u);
-      kv = kv + negIf(tb[(d.z >> 16) & 0xffu], (neg >> 6) & 1u);
-      kv = kv + negIf(tb[d.z >> 24], (neg >> 7) & 1u);
-      kv = kv + negIf(tb[d.w & 0xffu], (neg >> 8) & 1u);
+      auto acc = sumStart(negIf(tb[d.y & 0xffu], neg & 1u));
+      sumAdd(acc, negIf(tb[(d.y >> 8) & 0xffu], (neg >> 1) & 1u));
+      sumAdd(acc, negIf(tb[(d.y >> 16) & 0xffu], (neg >> 2) & 1u));
+      sumAdd(acc, negIf(tb[d.y >> 24], (neg >> 3) & 1u));
+      sumAdd(acc, negIf(tb[d.z & 0xffu], (neg >> 4) & 1u));
+      sumAdd(acc, negIf(tb[(d.z >> 8) & 0xffu], (neg >> 5) & 1u));
+      sumAdd(acc, negIf(tb[(d.z >> 16) & 0xffu], (neg >> 6) & 1u));
+      sumAdd(acc, negIf(tb[d.z >> 24], (neg >> 7) & 1u));
+      sumAdd(acc, negIf(tb[d.w & 0xffu], (neg >> 8) & 1u));
+      kv = sumEnd(acc);
     }
     if (needM)
     {
       uint32_t const mo = d.w >> 8;
       T const alpha = cx == 2 ? cst<T>(AB) : cst<T>(kAlpha01);
       T const beta = negIf(cx == 2 ? cst<T>(0.0) : cst<T>(kBeta0), cx == 1);
-      mv = alpha * tb[mo] + beta * tb[mo + 12];
+      mv = dot2(alpha, tb[mo], beta, tb[mo + 12]);
     }
     bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
 #pragma unroll
@@ -1024,7 +1025,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       LhsDev const & op = a.op[m];
       if (!op.on)
         continue;
-      T const v = op.stiff ? (op.mass ? ks[m] * kv + ms[m] * mv : ks[m] * kv) : ms[m] * mv;
+      T const v = op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv;
       double const val = toDouble(v);
       if (!live)
         continue;
