@@ -22,6 +22,7 @@
 //  - errors throw proxgpu::Error (carrying the pxg_status) instead of aborting.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <stdexcept>
@@ -201,6 +202,16 @@ struct FESpace
           "pxg_set_mesh");
     check(pxg_build_dofmap(ctx, &dof.size), ctx, "pxg_build_dofmap");
     check(pxg_build_pattern(ctx, &nnz), ctx, "pxg_build_pattern");
+    // boundary facets marked on the planes of the bounding box, as markFacetsCube does
+    // for buildHyperCube (include/mesh.hpp:443-481)
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (size_t k = 0; k < m.xyz.size(); ++k)
+    {
+      lo[k % 3] = std::min(lo[k % 3], m.xyz[k]);
+      hi[k % 3] = std::max(hi[k % 3], m.xyz[k]);
+    }
+    double const len[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    check(pxg_mark_facets_box(ctx, lo, len), ctx, "pxg_mark_facets_box");
   }
   FESpace(FESpace const &) = delete;
   FESpace & operator=(FESpace const &) = delete;
@@ -220,34 +231,21 @@ struct FESpace
   }
 };
 
-// BCEss{feSpace, marker} (include/bc.hpp:81-97) on the structured unit cube: the DOFs of
-// the facets with that marker, i.e. the DOFs on its plane; `value` is constant.
+// BCEss{feSpace, marker, value} (include/bc.hpp:81-97): the DOFs of the boundary facets
+// with that marker, set up on the device (pxg_set_bc_markers); or an explicit DOF list.
 struct BCEss
 {
+  int marker = side::NONE; // NONE: the explicit list below
+  double value = 0.0;
   std::vector<uint32_t> dofs;
   std::vector<double> values;
   double diag = 1.0; // BCEss::diag (bc.hpp:301)
 
   template <typename FE>
-  BCEss(FE const & fe, int marker, double value = 0.0)
+  BCEss(FE const &, int m, double v = 0.0): marker(m), value(v)
   {
-    int fn = PXG_FN_COORD_X;
-    double plane = 0.0;
-    switch (marker)
-    {
-    case side::BOTTOM: fn = PXG_FN_COORD_Y, plane = 0.0; break;
-    case side::RIGHT: fn = PXG_FN_COORD_X, plane = 1.0; break;
-    case side::TOP: fn = PXG_FN_COORD_Y, plane = 1.0; break;
-    case side::LEFT: fn = PXG_FN_COORD_X, plane = 0.0; break;
-    case side::BACK: fn = PXG_FN_COORD_Z, plane = 0.0; break;
-    case side::FRONT: fn = PXG_FN_COORD_Z, plane = 1.0; break;
-    default: throw Error(PXG_ERR_INVALID_ARG, "BCEss: unknown side marker");
-    }
-    std::vector<double> const c = fe.interpolate(fn);
-    for (size_t d = 0; d < c.size(); ++d)
-      if (std::fabs(c[d] - plane) <= 1e-6)
-        dofs.push_back((uint32_t)d);
-    values.assign(dofs.size(), value);
+    if (m < side::BOTTOM || m > side::FRONT)
+      throw Error(PXG_ERR_INVALID_ARG, "BCEss: unknown side marker");
   }
   BCEss(std::vector<uint32_t> d, std::vector<double> v): dofs(std::move(d)), values(std::move(v)) {}
 };
@@ -376,14 +374,36 @@ struct Builder
 private:
   void setBcs(std::vector<BCEss> const & bcs)
   {
+    size_t nm = 0;
+    double diag = 1.0;
+    for (auto const & bc: bcs)
+    {
+      nm += bc.marker != side::NONE;
+      diag = bc.diag;
+    }
+    if (nm && nm != bcs.size())
+      throw Error(PXG_ERR_UNSUPPORTED, "BCEss: marker and DOF-list conditions in one call");
+    if (nm)
+    {
+      // on the device: the marked facets' DOFs, constant values (later ones win)
+      std::vector<int32_t> m, f;
+      std::vector<double> c;
+      for (auto const & bc: bcs)
+      {
+        m.push_back(bc.marker);
+        f.push_back(PXG_FN_CONST);
+        c.push_back(bc.value);
+      }
+      check(pxg_set_bc_markers(fe.ctx, m.data(), f.data(), c.data(), (int)m.size(), diag), fe.ctx,
+            "pxg_set_bc_markers");
+      return;
+    }
     std::vector<uint32_t> d;
     std::vector<double> v;
-    double diag = 1.0;
     for (auto const & bc: bcs)
     {
       d.insert(d.end(), bc.dofs.begin(), bc.dofs.end());
       v.insert(v.end(), bc.values.begin(), bc.values.end());
-      diag = bc.diag;
     }
     check(pxg_set_bc(fe.ctx, d.data(), v.data(), (int64_t)d.size(), diag, PXG_MEM_HOST), fe.ctx, "pxg_set_bc");
   }

@@ -183,6 +183,40 @@ pxg_status pxg_set_coef(pxg_ctx * ctx, const double * k_e, int mem, void * strea
 pxg_status pxg_set_bc(pxg_ctx * ctx, const uint32_t * dofs, const double * vals, int64_t n,
                       double diag, int mem);
 
+/* ------------------------------------------------- boundary facets and BCs
+ * Device versions of proxpde's buildFacets / markFacetsCube (include/mesh.hpp:226-498)
+ * and BCEss::setupDofMap (include/bc.hpp:252-295).  Markers use proxpde's side
+ * numbering (mesh.hpp:178-188). */
+typedef enum pxg_side
+{
+  PXG_SIDE_NONE = 0,
+  PXG_SIDE_BOTTOM = 1, /* y = min */
+  PXG_SIDE_RIGHT = 2,  /* x = max */
+  PXG_SIDE_TOP = 3,    /* y = max */
+  PXG_SIDE_LEFT = 4,   /* x = min */
+  PXG_SIDE_BACK = 5,   /* z = min */
+  PXG_SIDE_FRONT = 6   /* z = max */
+} pxg_side;
+
+/* Boundary facets of the mesh (faces of exactly one element), kept on the device in
+ * the order of their sorted vertex ids; their count. */
+pxg_status pxg_build_facets(pxg_ctx * ctx, int64_t * nfacets);
+/* Host copies: faces[k] = element * (4 or 6) + local face (tetrahedron face i is
+ * opposite vertex i; hexahedron faces are {0,3,2,1}, {3,0,4,7}, {0,1,5,4}, {1,2,6,5},
+ * {2,3,7,6}, {4,5,6,7}), markers[k]; either pointer may be NULL. */
+pxg_status pxg_get_facets(pxg_ctx * ctx, uint32_t * faces, int32_t * markers);
+/* Markers given by the caller, one per facet in pxg_get_facets order (host array). */
+pxg_status pxg_set_facet_markers(pxg_ctx * ctx, const int32_t * markers);
+/* markFacetsCube: builds the facets if needed and marks those on the planes of the box
+ * [origin, origin + length] (first match in the order BOTTOM, RIGHT, TOP, LEFT, BACK,
+ * FRONT; tolerance 1e-6 of the length). */
+pxg_status pxg_mark_facets_box(pxg_ctx * ctx, const double * origin, const double * length);
+/* Dirichlet conditions from markers (replaces any earlier pxg_set_bc): condition k
+ * constrains the DOFs on the facets with markers[k] to coefs[k] * fns[k](DOF point);
+ * later conditions win on shared DOFs.  diag as in pxg_set_bc. */
+pxg_status pxg_set_bc_markers(pxg_ctx * ctx, const int32_t * markers, const int32_t * fns,
+                              const double * coefs, int nbc, double diag);
+
 /* --------------------------------------------------------------- assembly
  * One fused pass over the elements: up to two matrices (vals0/vals1, each nnz long on
  * the structural pattern, device memory) and one load vector b (ndof, device).

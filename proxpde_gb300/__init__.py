@@ -110,6 +110,7 @@ class FESpace:
         self.dof = _Dof(self)
         self._pattern = False
         self._bc_key = None
+        self._marked = False
 
     def pattern(self):
         if not self._pattern:
@@ -124,12 +125,38 @@ class FESpace:
     def set_coefficient(self, k_e):
         self.ctx.set_coef(np.ascontiguousarray(k_e, dtype=np.float64))
 
+    def mark_facets(self):
+        """Boundary facet markers on the device: the mesh's tagged facets, else the planes
+        of its bounding box (markFacetsCube, include/mesh.hpp:443-481)."""
+        if self._marked:
+            return
+        m = self.mesh
+        if m.facets is None:
+            lo, hi = m.xyz.min(axis=0), m.xyz.max(axis=0)
+            self.ctx.mark_facets_box(lo, hi - lo)
+        else:
+            faces, _ = self.ctx.get_facets()
+            hex_ = self.etype in (Q1HEX, Q2HEX)
+            nf = 6 if hex_ else 4
+            table = np.array(HEX_FACES if hex_ else [[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]])
+            e, lf = faces // nf, faces % nf
+            verts = np.sort(m.conn[e[:, None], table[lf]], axis=1)
+            fverts, tags = m.facets
+            lookup = {tuple(v[:3]): t for v, t in zip(np.sort(fverts, axis=1).tolist(), tags.tolist())}
+            markers = np.array([lookup.get(tuple(v[:3]), 0) for v in verts.tolist()], dtype=np.int32)
+            self.ctx.set_facet_markers(markers)
+        self._marked = True
+
     def apply_bcs(self, bcs):
         key = tuple(id(b) for b in bcs)
         if key == self._bc_key:
             return
         if not bcs:
             self.ctx.set_bc(np.zeros(0, np.uint32), np.zeros(0), 1.0)
+        elif all(b.marker is not None for b in bcs):
+            # marked facets -> constrained DOFs on the device (BCEss::setupDofMap)
+            self.mark_facets()
+            self.ctx.set_bc_markers([(b.marker, FN_CONST, b.value) for b in bcs], bcs[-1].diag)
         else:
             dofs = np.concatenate([b.dofs for b in bcs]).astype(np.uint32)
             vals = np.concatenate([b.values for b in bcs])
@@ -161,18 +188,35 @@ def _interp_coord(fe, d):
     return out
 
 
+HEX_FACES = [[0, 3, 2, 1], [3, 0, 4, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [4, 5, 6, 7]]
+
+
 class BCEss:
     """Essential BC on the DOFs of the boundary facets with a marker (bc.hpp:252-295),
-    or on an explicit DOF list.  ``value`` is a constant or an array per DOF."""
+    set up on the device from the facet markers; or on an explicit DOF list.  ``value``
+    is a constant (marker form) or an array per DOF (list form)."""
 
     def __init__(self, fe: FESpace, marker=None, value=0.0, dofs=None, diag=1.0):
         self.fe = fe
         self.diag = float(diag)
+        self._dofs = None
         if dofs is None:
-            dofs = self._marker_dofs(fe, marker)
-        self.dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
-        v = np.asarray(value, dtype=np.float64)
-        self.values = np.broadcast_to(v, self.dofs.shape).copy() if v.ndim == 0 else v.copy()
+            if marker is None or np.ndim(value) != 0:
+                raise ValueError("BCEss: a marker with a constant value, or a DOF list")
+            self.marker, self.value = int(marker), float(value)
+        else:
+            self.marker = None
+            self._dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
+            v = np.asarray(value, dtype=np.float64)
+            self.values = np.broadcast_to(v, self._dofs.shape).copy() if v.ndim == 0 else v.copy()
+
+    @property
+    def dofs(self):
+        """The constrained DOFs (host computation, for inspection)."""
+        if self._dofs is None:
+            self._dofs = self._marker_dofs(self.fe, self.marker)
+            self.values = np.full(self._dofs.shape, self.value)
+        return self._dofs
 
     @staticmethod
     def _marker_dofs(fe, marker):

@@ -29,6 +29,7 @@ EXPORTS = [
     "pxg_set_mesh", "pxg_set_coords", "pxg_build_dofmap", "pxg_set_dofmap", "pxg_get_dofmap",
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
     "pxg_assemble", "pxg_prune_count", "pxg_prune_count_device", "pxg_set_scatter", "pxg_colouring", "pxg_autotune",
+    "pxg_build_facets", "pxg_get_facets", "pxg_set_facet_markers", "pxg_mark_facets_box", "pxg_set_bc_markers",
     "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
     "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
@@ -109,6 +110,11 @@ def load(path: str = LIB_PATH):
         "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
         "pxg_prune_count_device": ([vp, vp, vp, vp], C.c_int),
         "pxg_set_scatter": ([vp, C.c_int, C.c_int], C.c_int),
+        "pxg_build_facets": ([vp, i64p], C.c_int),
+        "pxg_get_facets": ([vp, vp, vp], C.c_int),
+        "pxg_set_facet_markers": ([vp, vp], C.c_int),
+        "pxg_mark_facets_box": ([vp, vp, vp], C.c_int),
+        "pxg_set_bc_markers": ([vp, vp, vp, vp, C.c_int, C.c_double], C.c_int),
         "pxg_colouring": ([vp, C.POINTER(C.c_int), vp, vp], C.c_int),
         "pxg_autotune": ([vp, C.POINTER(LhsOp), C.POINTER(LhsOp), C.POINTER(RhsOp), C.POINTER(TuneReport)], C.c_int),
         "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
@@ -269,6 +275,38 @@ class Context:
         """Asynchronous prune count into `out` (a one-element int64 device tensor)."""
         assert str(out.dtype) == "torch.int64" and out.is_cuda and out.numel() >= 1
         self._check(self.L.pxg_prune_count_device(self.h, _ptr(vals), _ptr(out), stream), "prune_count_device")
+
+    # --- boundary facets and Dirichlet conditions from markers (on the device)
+    def build_facets(self):
+        n = C.c_int64()
+        self._check(self.L.pxg_build_facets(self.h, C.byref(n)), "build_facets")
+        self.nfacets = n.value
+        return n.value
+
+    def get_facets(self):
+        """(faces: element * faces-per-element + local face, markers), in device order"""
+        n = self.build_facets()
+        faces = np.empty(n, dtype=np.uint32)
+        markers = np.empty(n, dtype=np.int32)
+        self._check(self.L.pxg_get_facets(self.h, faces.ctypes.data, markers.ctypes.data), "get_facets")
+        return faces, markers
+
+    def set_facet_markers(self, markers):
+        markers = np.ascontiguousarray(markers, dtype=np.int32)
+        self._check(self.L.pxg_set_facet_markers(self.h, markers.ctypes.data), "set_facet_markers")
+
+    def mark_facets_box(self, origin=(0.0, 0.0, 0.0), length=(1.0, 1.0, 1.0)):
+        o = np.ascontiguousarray(origin, dtype=np.float64)
+        ln = np.ascontiguousarray(length, dtype=np.float64)
+        self._check(self.L.pxg_mark_facets_box(self.h, o.ctypes.data, ln.ctypes.data), "mark_facets_box")
+
+    def set_bc_markers(self, conditions, diag=1.0):
+        """conditions: [(marker, fn id, coef)]; DOFs on the marked facets get coef * fn(x)."""
+        m = np.ascontiguousarray([c[0] for c in conditions], dtype=np.int32)
+        f = np.ascontiguousarray([c[1] for c in conditions], dtype=np.int32)
+        v = np.ascontiguousarray([c[2] for c in conditions], dtype=np.float64)
+        self._check(self.L.pxg_set_bc_markers(self.h, m.ctypes.data, f.ctypes.data, v.ctypes.data, len(conditions),
+                                              float(diag)), "set_bc_markers")
 
     # --- scatter strategy and autotuning
     def set_scatter(self, scatter, threads=0):

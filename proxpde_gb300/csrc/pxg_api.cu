@@ -187,6 +187,10 @@ pxg_status pxg_set_mesh(pxg_ctx * c, int etype, double const * xyz, int64_t nnod
   c->colour.start.clear();
   c->colour.ncol = 0;
   c->colour.built = false;
+  c->facets.face.reset();
+  c->facets.marker.reset();
+  c->facets.n = 0;
+  c->facets.built = false;
   c->scatter = PXG_SCATTER_REDUCE;
   c->threads = 0;
   c->bcMask.reset();

@@ -309,6 +309,14 @@ struct pxg_ctx
     pxg::DevBuf<uint32_t> perm;
     bool built = false;
   } colour;
+  // boundary facets in key order: element * faces-per-element + local face, and markers
+  struct FacetState
+  {
+    bool built = false;
+    int64_t n = 0;
+    pxg::DevBuf<uint32_t> face;
+    pxg::DevBuf<int32_t> marker;
+  } facets;
   // Q1 hexahedra use the tensor-product kernel in double-float arithmetic; in the
   // environment PXG_Q1_FP64=1 selects its FP64 variant and PXG_Q1_GENERIC=1 the
   // generic kernel (both kept for cross-checks)
