@@ -217,6 +217,40 @@ pxg_status pxg_mark_facets_box(pxg_ctx * ctx, const double * origin, const doubl
 pxg_status pxg_set_bc_markers(pxg_ctx * ctx, const int32_t * markers, const int32_t * fns,
                               const double * coefs, int nbc, double diag);
 
+/* ------------------------------------------ systems of spaces on one mesh
+ * Vector spaces and mixed (coupled) problems: FESpace<..., dim> with its offset
+ * (include/fespace.hpp:15-60), Builder::buildLhs on vector spaces and
+ * Builder::buildCoupling (include/builder.hpp:31-277).  The spaces are contexts with
+ * DOF maps on the same mesh; space s gets dims[s] components in BLOCK ordering
+ * (component d of DOF k is k + d * ndof_s) and the offset of the spaces before it. */
+typedef struct pxg_sys pxg_sys;
+
+typedef enum pxg_op_kind
+{
+  PXG_OP_STIFFNESS = 1,        /* AssemblyStiffness on each component (assembly_lhs.hpp:52-65) */
+  PXG_OP_TENSOR_STIFFNESS = 2, /* AssemblyTensorStiffness (assembly_lhs.hpp:116-161) */
+  PXG_OP_MASS = 3,             /* AssemblyMass on each component (assembly_lhs.hpp:347-365) */
+  PXG_OP_GRAD = 4,             /* AssemblyGrad: rows vector space, columns scalar space (assembly_coupling.hpp:42-86) */
+  PXG_OP_DIV = 5               /* AssemblyDiv: rows scalar space, columns vector space (assembly_coupling.hpp:89-132) */
+} pxg_op_kind;
+
+/* Build the system and its pattern (all DOF pairs of each element over all spaces; the
+ * blocks the reference leaves empty are structural zeros that the prune removes).
+ * qr_types[s]: element type whose quadrature rule space s uses (NULL: its own), e.g.
+ * the pressure space of a Taylor-Hood pair on the velocity's rule. */
+pxg_status pxg_sys_create(pxg_sys ** sys, pxg_ctx * const * spaces, const int * dims, const int * qr_types,
+                          int nspaces, int64_t * ntot, int64_t * nnz);
+pxg_status pxg_sys_destroy(pxg_sys * sys);
+pxg_status pxg_sys_get_pattern(pxg_sys * sys, int32_t * row_ptr, int32_t * col_idx);
+pxg_status pxg_sys_pattern_device(pxg_sys * sys, const int32_t ** row_ptr, const int32_t ** col_idx);
+/* Dirichlet data of one space over its component DOFs (host arrays; the last value wins). */
+pxg_status pxg_sys_set_bc(pxg_sys * sys, int space, const uint32_t * dofs, const double * vals, int64_t n,
+                          double diag);
+/* One Builder call: row == col is buildLhs (constrained diagonal = diag, b = h there),
+ * row != col buildCoupling (no diagonal); vals (nnz) and b (ntot) are device arrays. */
+pxg_status pxg_sys_assemble(pxg_sys * sys, int row, int col, const int * kinds, const double * coefs, int nops,
+                            double * vals, double * b, unsigned flags, void * stream);
+
 /* --------------------------------------------------------------- assembly
  * One fused pass over the elements: up to two matrices (vals0/vals1, each nnz long on
  * the structural pattern, device memory) and one load vector b (ndof, device).

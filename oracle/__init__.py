@@ -92,6 +92,12 @@ def lib():
         L.orc_csr_copy.argtypes = [C.c_void_p, i32p, i32p, dp]
         L.orc_csr_free.argtypes = [C.c_void_p]
         L.orc_adjoint_grad.argtypes = [C.c_int, dp, up, C.c_int64, up, dp, u8p, dp, dp, C.c_int, dp]
+        vp = C.c_void_p
+        L.orc_system_call.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, C.c_double, dp, up,
+                                      C.c_int64, C.c_int, vp, vp, dp]
+        L.orc_system_call.restype = vp
+        L.orc_system_close.argtypes = [vp, C.c_int64]
+        L.orc_system_close.restype = vp
         _lib = L
     return _lib
 
@@ -319,3 +325,129 @@ def poisson_golden(t, xyz, conn, bc_mask_fn, rhs_kind="analytic"):
     u = spla.spsolve(A, b)
     ex = interpolate(t, xyz, conn, em, ndof, FN_POISSON_EXACT)
     return float(np.linalg.norm(u - ex))
+
+
+# ------------------------------------------------------------ vector spaces / coupling
+# Assembly kinds of orc_system_call (oracle.cpp): stiffness, tensor stiffness, mass,
+# grad (rows: vector space, columns: scalar space), div (rows: scalar, columns: vector).
+STIFF, TENSOR_STIFF, MASS, GRAD, DIV = 1, 2, 3, 4, 5
+
+
+class System:
+    """FE spaces on one mesh with offsets in one global system (FESpace<..., dim>,
+    BLOCK ordering) and Builder calls over them (buildLhs / buildCoupling); close()
+    is closeMatrix.  spaces: list of dict(t, qr, dim, offset, ndof, em)."""
+
+    def __init__(self, xyz, conn, spaces, ntot):
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.uint32)
+        self.spaces = spaces
+        self.ntot = int(ntot)
+        self.b = np.zeros(self.ntot)
+        self._acc = None
+        self.bc = [(None, None) for _ in spaces]
+        self.diag = 1.0
+
+    def set_bc(self, s, mask, vals, diag=1.0):
+        """mask / vals over the space's ndof * dim component DOFs (id + d * ndof)."""
+        self.bc[s] = (np.ascontiguousarray(mask, dtype=np.uint8), np.ascontiguousarray(vals, dtype=np.float64))
+        self.diag = float(diag)
+
+    def call(self, row, col, ops):
+        sp = self.spaces
+        n = len(sp)
+        arr = lambda ty, xs: (ty * n)(*xs)
+        ts = np.array([x["t"] for x in sp], dtype=np.int32)
+        qs = np.array([x["qr"] for x in sp], dtype=np.int32)
+        dims = np.array([x["dim"] for x in sp], dtype=np.int32)
+        offs = np.array([x["offset"] for x in sp], dtype=np.int64)
+        nd = np.array([x["ndof"] for x in sp], dtype=np.int64)
+        ems = [np.ascontiguousarray(x["em"], dtype=np.uint32) for x in sp]
+        em_p = arr(C.c_void_p, [e.ctypes.data for e in ems])
+        mk_p = arr(C.c_void_p, [m.ctypes.data if m is not None else None for m, _ in self.bc])
+        vl_p = arr(C.c_void_p, [v.ctypes.data if v is not None else None for _, v in self.bc])
+        kinds = np.array([k for k, _ in ops], dtype=np.int32)
+        coefs = np.array([c for _, c in ops], dtype=np.float64)
+        acc = lib().orc_system_call(self._acc, int(row), int(col), ts.ctypes.data, qs.ctypes.data, dims.ctypes.data,
+                                    offs.ctypes.data, nd.ctypes.data, em_p, mk_p, vl_p, self.diag, _dp(self.xyz),
+                                    _up(self.conn), self.conn.shape[0], len(ops), kinds.ctypes.data,
+                                    coefs.ctypes.data, _dp(self.b))
+        if not acc:
+            raise ValueError("orc_system_call: unknown assembly kind")
+        self._acc = acc
+
+    def close(self):
+        h = lib().orc_system_close(self._acc, self.ntot)
+        self._acc = None
+        nnz = lib().orc_csr_nnz(h)
+        rp = np.zeros(self.ntot + 1, dtype=np.int32)
+        col = np.zeros(nnz, dtype=np.int32)
+        val = np.zeros(nnz)
+        lib().orc_csr_copy(h, _p(rp, C.c_int32), _p(col, C.c_int32), _dp(val))
+        lib().orc_csr_free(h)
+        return rp, col, val
+
+
+def stokes_problem(elem, n=4, ly=2.0):
+    """The mesh, spaces and Dirichlet data of proxpde's test/stokes3dhex.cpp and
+    stokes3dtet.cpp: Taylor-Hood Q2-Q1 (P2-P1) on the box [0,1] x [0,ly] x [0,1] with
+    n^3 cells; BCEss BOTTOM inlet (0, (1 - x^2) / 2, 0), RIGHT zero, TOP / LEFT zero on
+    components 0, 2, BACK / FRONT zero on component 2 (the last value wins)."""
+    if elem == "hex":
+        xyz, conn = cube_hex(n)
+        tv, tp = Q2HEX, Q1HEX
+    else:
+        xyz, conn = cube_tet5(n)
+        tv, tp = P2TET, P1TET
+    xyz = xyz.copy()
+    xyz[:, 1] *= ly
+    emv, ndv = dofmap(tv, xyz.shape[0], conn)
+    emp, ndp = dofmap(tp, xyz.shape[0], conn)
+    xv = dof_coords(tv, xyz, conn, emv, ndv)
+    xp = dof_coords(tp, xyz, conn, emp, ndp)
+    inlet = lambda X: np.stack([np.zeros(len(X)), 0.5 * (1.0 - X[:, 0] ** 2), np.zeros(len(X))], axis=1)
+    zero = lambda X: np.zeros((len(X), 3))
+    on = lambda a, v: np.abs(xv[:, a] - v) <= 1e-12
+    bcs = [(on(1, 0.0), inlet, (0, 1, 2)), (on(0, 1.0), zero, (0, 1, 2)), (on(1, ly), zero, (0, 2)),
+           (on(0, 0.0), zero, (0, 2)), (on(2, 0.0), zero, (2,)), (on(2, 1.0), zero, (2,))]
+    mask = np.zeros(3 * ndv, dtype=np.uint8)
+    vals = np.zeros(3 * ndv)
+    for sel, f, comps in bcs:
+        ids = np.nonzero(sel)[0]
+        fv = f(xv[ids])
+        for c in comps:
+            mask[ids + c * ndv] = 1
+            vals[ids + c * ndv] = fv[:, c]
+    return dict(xyz=xyz, conn=conn, tv=tv, tp=tp, emv=emv, ndv=ndv, emp=emp, ndp=ndp, xv=xv, xp=xp,
+                bc_mask=mask, bc_vals=vals, u_exact=inlet(xv), ly=ly)
+
+
+def stokes_errors(P, sol, nu=0.1):
+    """||u - u_ex||, ||v - v_ex||, ||w - w_ex||, ||p - p_ex|| (p_ex = nu (ly - y))."""
+    ndv = P["ndv"]
+    err = [float(np.linalg.norm(sol[c * ndv:(c + 1) * ndv] - P["u_exact"][:, c])) for c in range(3)]
+    err.append(float(np.linalg.norm(sol[3 * ndv:] - nu * (P["ly"] - P["xp"][:, 1]))))
+    return err
+
+
+def stokes_golden(elem, n=4, ly=2.0, nu=0.1):
+    """proxpde's test/stokes3dhex.cpp / stokes3dtet.cpp through the oracle: tensor
+    stiffness on the velocity, grad / div couplings with the pressure, a direct solve;
+    returns the four error norms (pinned at stokes3dhex.cpp:135-140,
+    stokes3dtet.cpp:122-127), the closed matrix and b."""
+    import scipy.sparse.linalg as spla
+
+    P = stokes_problem(elem, n, ly)
+    ndv, ndp = P["ndv"], P["ndp"]
+    spaces = [dict(t=P["tv"], qr=P["tv"], dim=3, offset=0, ndof=ndv, em=P["emv"]),
+              dict(t=P["tp"], qr=P["tv"], dim=1, offset=3 * ndv, ndof=ndp, em=P["emp"])]
+    ntot = 3 * ndv + ndp
+    S = System(P["xyz"], P["conn"], spaces, ntot)
+    S.set_bc(0, P["bc_mask"], P["bc_vals"], 1.0)
+    S.call(0, 0, [(TENSOR_STIFF, nu)])
+    S.call(0, 1, [(GRAD, -1.0)])
+    S.call(1, 0, [(DIV, -1.0)])
+    rp, col, val = S.close()
+    A = csr_to_scipy((rp, col, val), ntot).tocsc()
+    sol = spla.spsolve(A, S.b)
+    return stokes_errors(P, sol, nu), (rp, col, val), S.b

@@ -271,7 +271,7 @@ void origin(int t, double const (*X)[3], double * o)
 // -------------------------------------------------------------------- CurFE
 struct CurFE
 {
-  int t, N, nq;
+  int t, qrt, N, nq; // element type, element type whose rule is used (FESpace's QR)
   // constant tables (curfe.hpp:20-45)
   std::vector<double> phiRef;  // nq x N
   std::vector<double> dphiRef; // nq x N x 3 (also the mapping table: mapping = dphiFun)
@@ -281,12 +281,13 @@ struct CurFE
   std::vector<double> dphi;  // nq x N x 3
   std::vector<double> dofPts; // N x 3
 
-  explicit CurFE(int type): t(type), N(numDofs(type)), nq(rule(type).n)
+  explicit CurFE(int type, int qrType = -1):
+      t(type), qrt(qrType < 0 ? type : qrType), N(numDofs(type)), nq(rule(qrt).n)
   {
     phiRef.resize(nq * N);
     dphiRef.resize(nq * N * 3);
     for (int q = 0; q < nq; ++q)
-      shape(t, rule(t).node[q].data(), &phiRef[q * N], &dphiRef[q * N * 3]);
+      shape(t, rule(qrt).node[q].data(), &phiRef[q * N], &dphiRef[q * N * 3]);
     JxW.resize(nq);
     qpt.resize(nq * 3);
     dphi.resize(nq * N * 3);
@@ -300,7 +301,7 @@ struct CurFE
     mappingPoints(t, X, P);
     double o[3];
     origin(t, X, o);
-    QRule const & qr = rule(t);
+    QRule const & qr = rule(qrt);
     for (int q = 0; q < nq; ++q)
     {
       double J[3][3] = {};
@@ -942,6 +943,208 @@ int orc_adjoint_grad(int t, double const * xyz, uint32_t const * conn, int64_t n
     g[e] = -s;
   }
   return 0;
+}
+
+} // extern "C"
+
+// ====================================================== vector spaces and coupling
+// A system of FE spaces on one mesh (FESpace<..., dim> with its offset in the global
+// vector, include/fespace.hpp:15-60; BLOCK DOF ordering: component d of local DOF i is
+// elemMap(e, i) + d * ndof, include/dof.hpp:312-327) and one Builder call over it:
+//   - buildLhs (row space == column space, include/builder.hpp:31-154): Diagonal
+//     assemblies, Dirichlet condensation with the diagonal set on constrained DOFs;
+//   - buildCoupling (include/builder.hpp:156-277): rows of one space, columns of
+//     another, Fe = -Crow Ke h, Ke = Crow Ke Cclm, no diagonal.
+// Assemblies (coef c; JxW, dphi, phi of the row space's CurFE unless stated):
+//   1 AssemblyStiffness       Ke(i+dN, j+dN)   += c JxW dphi_i . dphi_j          (assembly_lhs.hpp:52-65)
+//   2 AssemblyTensorStiffness Ke(i+dN, j+dN)   += c JxW dphi_i . dphi_j,
+//                             Ke(i+d1N, j+d2N) += c JxW dphi_i[d1] dphi_j[d2]    (assembly_lhs.hpp:116-161)
+//   3 AssemblyMass            Ke(i+dN, j+dN)   += c JxW phi_i phi_j              (assembly_lhs.hpp:347-365)
+//   4 AssemblyGrad            Ke(i+dN, j)      += c JxW dphi_i[d] psi_j          (assembly_coupling.hpp:42-86)
+//   5 AssemblyDiv             Ke(i, j+dN)      += c JxW phi_i dpsi_j[d]          (assembly_coupling.hpp:89-132)
+// (psi: the column space's functions at the same quadrature points.)  The triplets
+// of the call are returned in emission order; orc_system_close sums and prunes them.
+namespace
+{
+struct SysTrip
+{
+  std::vector<OrcTriplet> t;
+};
+} // namespace
+
+extern "C"
+{
+
+// Space s: type ts[s], quadrature of type qs[s], dims[s] components, offsets[s],
+// ndofs[s] scalar DOFs, elemMaps[s] (nelem x numDofs(ts[s])), optional BC mask and
+// values over its ndofs[s] * dims[s] component DOFs.  ops: kinds[k], coefs[k].
+void * orc_system_call(void * acc, int row, int col, int const * ts, int const * qs, int const * dims,
+                       int64_t const * offsets, int64_t const * ndofs, uint32_t const * const * elemMaps,
+                       uint8_t const * const * bcMask, double const * const * bcVal, double bcDiag,
+                       double const * xyz, uint32_t const * conn, int64_t nelem, int nops, int const * kinds,
+                       double const * coefs, double * b)
+{
+  auto * T = acc ? static_cast<SysTrip *>(acc) : new SysTrip;
+  int const tr = ts[row], tc = ts[col], dr = dims[row], dc = dims[col];
+  int const Nr = numDofs(tr), Nc = numDofs(tc), Lr = Nr * dr, Lc = Nc * dc;
+  int const nv = numVerts(tr);
+  bool const diagCall = row == col;
+  CurFE fr(tr, qs[row]), fc(tc, qs[col]);
+  std::vector<double> Ke((size_t)Lr * Lc), Fe(Lr), h(Lc);
+  std::vector<char> consR(Lr), consC(Lc);
+  for (int64_t e = 0; e < nelem; ++e)
+  {
+    double X[8][3];
+    for (int v = 0; v < nv; ++v)
+      for (int d = 0; d < 3; ++d)
+        X[v][d] = xyz[3 * (int64_t)conn[e * nv + v] + d];
+    fr.reinit(X);
+    if (!diagCall)
+      fc.reinit(X);
+    std::fill(Ke.begin(), Ke.end(), 0.);
+    for (int k = 0; k < nops; ++k)
+    {
+      double const c = coefs[k];
+      for (int q = 0; q < fr.nq; ++q)
+      {
+        double const w = c * fr.JxW[q];
+        double const * Dr = &fr.dphi[q * Nr * 3];
+        double const * Pr = &fr.phiRef[q * Nr];
+        double const * Dc = diagCall ? Dr : &fc.dphi[q * Nc * 3];
+        double const * Pc = diagCall ? Pr : &fc.phiRef[q * Nc];
+        switch (kinds[k])
+        {
+        case 1:
+        case 2:
+          for (int d = 0; d < dr; ++d)
+            for (int i = 0; i < Nr; ++i)
+              for (int j = 0; j < Nr; ++j)
+                Ke[(size_t)(i + d * Nr) * Lc + j + d * Nr] +=
+                    w * (Dr[3 * i] * Dr[3 * j] + Dr[3 * i + 1] * Dr[3 * j + 1] + Dr[3 * i + 2] * Dr[3 * j + 2]);
+          if (kinds[k] == 2)
+            for (int d1 = 0; d1 < dr; ++d1)
+              for (int d2 = 0; d2 < dr; ++d2)
+                for (int i = 0; i < Nr; ++i)
+                  for (int j = 0; j < Nr; ++j)
+                    Ke[(size_t)(i + d1 * Nr) * Lc + j + d2 * Nr] += w * Dr[3 * i + d1] * Dr[3 * j + d2];
+          break;
+        case 3:
+          for (int d = 0; d < dr; ++d)
+            for (int i = 0; i < Nr; ++i)
+              for (int j = 0; j < Nr; ++j)
+                Ke[(size_t)(i + d * Nr) * Lc + j + d * Nr] += w * Pr[i] * Pr[j];
+          break;
+        case 4:
+          for (int d = 0; d < dr; ++d)
+            for (int i = 0; i < Nr; ++i)
+              for (int j = 0; j < Nc; ++j)
+                Ke[(size_t)(i + d * Nr) * Lc + j] += w * Dr[3 * i + d] * Pc[j];
+          break;
+        case 5:
+          for (int d = 0; d < dc; ++d)
+            for (int i = 0; i < Nr; ++i)
+              for (int j = 0; j < Nc; ++j)
+                Ke[(size_t)i * Lc + j + d * Nc] += w * Pr[i] * Dc[3 * j + d];
+          break;
+        default:
+          return nullptr;
+        }
+      }
+    }
+    // constraints: component DOF of local (i, d) is elemMap(e, i) + d * ndof
+    uint32_t const * er = elemMaps[row] + e * Nr;
+    uint32_t const * ec = elemMaps[col] + e * Nc;
+    for (int d = 0; d < dr; ++d)
+      for (int i = 0; i < Nr; ++i)
+      {
+        int64_t const id = er[i] + (int64_t)d * ndofs[row];
+        consR[i + d * Nr] = bcMask[row] && bcMask[row][id];
+      }
+    for (int d = 0; d < dc; ++d)
+      for (int j = 0; j < Nc; ++j)
+      {
+        int64_t const id = ec[j] + (int64_t)d * ndofs[col];
+        consC[j + d * Nc] = bcMask[col] && bcMask[col][id];
+        h[j + d * Nc] = consC[j + d * Nc] ? bcVal[col][id] : 0.;
+      }
+    // Fe = -C Ke h ; Ke = C Ke C (rows / columns)
+    for (int I = 0; I < Lr; ++I)
+    {
+      double kh = 0.;
+      for (int J = 0; J < Lc; ++J)
+        kh += Ke[(size_t)I * Lc + J] * h[J];
+      Fe[I] = consR[I] ? 0. : (0. - kh);
+    }
+    for (int I = 0; I < Lr; ++I)
+      for (int J = 0; J < Lc; ++J)
+        if (consR[I] || consC[J])
+          Ke[(size_t)I * Lc + J] = 0.;
+    if (diagCall)
+      for (int I = 0; I < Lr; ++I)
+        if (consR[I])
+        {
+          Ke[(size_t)I * Lc + I] = bcDiag;
+          Fe[I] = h[I];
+        }
+    // emission (builder.hpp:139-152 / 254-274): i, d1, then j, d2
+    for (int i = 0; i < Nr; ++i)
+      for (int d1 = 0; d1 < dr; ++d1)
+      {
+        int32_t const idI = (int32_t)(offsets[row] + er[i] + (int64_t)d1 * ndofs[row]);
+        if (b)
+          b[idI] += Fe[i + d1 * Nr];
+        for (int j = 0; j < Nc; ++j)
+          for (int d2 = 0; d2 < dc; ++d2)
+          {
+            int32_t const idJ = (int32_t)(offsets[col] + ec[j] + (int64_t)d2 * ndofs[col]);
+            T->t.push_back({idI, idJ, Ke[(size_t)(i + d1 * Nr) * Lc + j + d2 * Nc]});
+          }
+      }
+  }
+  return T;
+}
+
+// closeMatrix over the accumulated calls: duplicates summed in emission order, columns
+// sorted, |v| <= 1e-16 pruned.  Frees the accumulator; returns a CSR handle.
+void * orc_system_close(void * acc, int64_t ntot)
+{
+  auto * T = static_cast<SysTrip *>(acc);
+  auto * out = new orc_csr;
+  out->n = ntot;
+  std::vector<std::vector<std::pair<int32_t, double>>> rows(ntot);
+  std::vector<int64_t> slot(ntot, -1);
+  if (T)
+    for (auto const & tr: T->t)
+    {
+      auto & R = rows[tr.r];
+      (void)slot;
+      bool found = false;
+      for (auto & pr: R)
+        if (pr.first == tr.c)
+        {
+          pr.second += tr.v;
+          found = true;
+          break;
+        }
+      if (!found)
+        R.emplace_back(tr.c, tr.v);
+    }
+  delete T;
+  out->rowPtr.assign(ntot + 1, 0);
+  for (int64_t r = 0; r < ntot; ++r)
+  {
+    auto & R = rows[r];
+    std::sort(R.begin(), R.end(), [](auto const & x, auto const & y) { return x.first < y.first; });
+    for (auto const & pr: R)
+      if (std::fabs(pr.second) > 1e-16)
+      {
+        out->col.push_back(pr.first);
+        out->val.push_back(pr.second);
+      }
+    out->rowPtr[r + 1] = (int32_t)out->col.size();
+  }
+  out->nnz = out->rowPtr[ntot];
+  return out;
 }
 
 } // extern "C"

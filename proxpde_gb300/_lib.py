@@ -30,6 +30,8 @@ EXPORTS = [
     "pxg_build_pattern", "pxg_get_pattern", "pxg_pattern_device", "pxg_set_coef", "pxg_set_bc",
     "pxg_assemble", "pxg_prune_count", "pxg_prune_count_device", "pxg_set_scatter", "pxg_colouring", "pxg_autotune",
     "pxg_build_facets", "pxg_get_facets", "pxg_set_facet_markers", "pxg_mark_facets_box", "pxg_set_bc_markers",
+    "pxg_sys_create", "pxg_sys_destroy", "pxg_sys_get_pattern", "pxg_sys_pattern_device", "pxg_sys_set_bc",
+    "pxg_sys_assemble",
     "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
     "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
@@ -110,6 +112,12 @@ def load(path: str = LIB_PATH):
         "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
         "pxg_prune_count_device": ([vp, vp, vp, vp], C.c_int),
         "pxg_set_scatter": ([vp, C.c_int, C.c_int], C.c_int),
+        "pxg_sys_create": ([C.POINTER(vp), vp, vp, vp, C.c_int, i64p, i64p], C.c_int),
+        "pxg_sys_destroy": ([vp], C.c_int),
+        "pxg_sys_get_pattern": ([vp, vp, vp], C.c_int),
+        "pxg_sys_pattern_device": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int),
+        "pxg_sys_set_bc": ([vp, C.c_int, vp, vp, i64, C.c_double], C.c_int),
+        "pxg_sys_assemble": ([vp, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp, C.c_uint, vp], C.c_int),
         "pxg_build_facets": ([vp, i64p], C.c_int),
         "pxg_get_facets": ([vp, vp, vp], C.c_int),
         "pxg_set_facet_markers": ([vp, vp], C.c_int),
@@ -365,3 +373,62 @@ class Context:
         self._check(self.L.pxg_adjoint_backward(self.h, float(dloss), _ptr(grad), _ptr(lam_out), C.byref(it),
                                                 stream), "adjoint_backward")
         return it.value
+
+
+OP_STIFFNESS, OP_TENSOR_STIFFNESS, OP_MASS, OP_GRAD, OP_DIV = 1, 2, 3, 4, 5
+
+
+class System:
+    """pxg_sys: spaces (contexts on one mesh with DOF maps) with dims, offsets in BLOCK
+    ordering, one pattern; assemble() is one Builder call over (row, col) spaces."""
+
+    def __init__(self, spaces, dims, qr_types=None):
+        self.L = load()
+        self.spaces = list(spaces)
+        self.dims = [int(d) for d in dims]
+        n = len(self.spaces)
+        ctxs = (C.c_void_p * n)(*[c.h.value for c in self.spaces])
+        d = np.ascontiguousarray(self.dims, dtype=np.int32)
+        q = None if qr_types is None else np.ascontiguousarray(qr_types, dtype=np.int32)
+        self.h = C.c_void_p()
+        nt, nz = C.c_int64(), C.c_int64()
+        st = self.L.pxg_sys_create(C.byref(self.h), ctxs, d.ctypes.data, None if q is None else q.ctypes.data, n,
+                                   C.byref(nt), C.byref(nz))
+        if st != 0:
+            raise PxgError(st, "pxg_sys_create: " + self.L.pxg_last_error(self.spaces[0].h).decode())
+        self.ntot, self.nnz = nt.value, nz.value
+        self.offsets = np.cumsum([0] + [c.ndof * dd for c, dd in zip(self.spaces, self.dims)])[:-1].tolist()
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.pxg_sys_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def _check(self, st, what, space=0):
+        if st != 0:
+            raise PxgError(st, f"{what}: " + self.L.pxg_last_error(self.spaces[space].h).decode())
+
+    def get_pattern(self):
+        rp = np.zeros(self.ntot + 1, dtype=np.int32)
+        ci = np.zeros(self.nnz, dtype=np.int32)
+        self._check(self.L.pxg_sys_get_pattern(self.h, rp.ctypes.data, ci.ctypes.data), "sys_get_pattern")
+        return rp, ci
+
+    def pattern_device(self):
+        rp, ci = C.c_void_p(), C.c_void_p()
+        self._check(self.L.pxg_sys_pattern_device(self.h, C.byref(rp), C.byref(ci)), "sys_pattern_device")
+        return rp.value, ci.value
+
+    def set_bc(self, space, dofs, vals, diag=1.0):
+        dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self._check(self.L.pxg_sys_set_bc(self.h, int(space), dofs.ctypes.data, vals.ctypes.data, dofs.size,
+                                          float(diag)), "sys_set_bc", space)
+
+    def assemble(self, row, col, ops, vals, b=None, accumulate=False, stream=None):
+        """ops: [(kind, coef)]; vals (nnz) and b (ntot) device tensors."""
+        k = np.ascontiguousarray([o[0] for o in ops], dtype=np.int32)
+        c = np.ascontiguousarray([o[1] for o in ops], dtype=np.float64)
+        self._check(self.L.pxg_sys_assemble(self.h, int(row), int(col), k.ctypes.data, c.ctypes.data, len(ops),
+                                            _ptr(vals), _ptr(b), ACCUMULATE if accumulate else 0, stream),
+                    "sys_assemble", row)

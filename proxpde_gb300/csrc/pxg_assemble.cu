@@ -225,6 +225,10 @@ void shapeHost(int t, double const * p, double * phi, double * dphi)
 int gTablesDone[64] = {0};
 } // namespace
 
+// the host restatements, for the tables of other translation units
+void hostRule(int t, std::vector<double> & xi, std::vector<double> & w) { ruleHost(t, xi, w); }
+void hostShape(int t, double const * p, double * phi, double * dphi) { shapeHost(t, p, phi, dphi); }
+
 pxg_status initTables(pxg_ctx * c)
 {
   if (c->device >= 0 && c->device < 64 && gTablesDone[c->device])

@@ -448,6 +448,10 @@ pxg_status buildPattern(pxg_ctx * c);
 
 // reference tables (pxg_assemble.cu)
 pxg_status initTables(pxg_ctx * c);
+// quadrature rule (nodes xi[3 q + d], weights) and shape functions of element type t
+// on the reference element, as proxpde defines them (host)
+void hostRule(int t, std::vector<double> & xi, std::vector<double> & w);
+void hostShape(int t, double const * p, double * phi, double * dphi);
 // g_e = -(C u)_e^T K_e (C lambda)_e for every element (pxg_assemble.cu)
 pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, double * g, cudaStream_t s);
 // Jacobi-PCG (pxg_solve.cu)

@@ -44,3 +44,18 @@ def test_unstructured_p1_golden(oracle_lib):
 
     val = O.poisson_golden(O.P1TET, xyz, conn, bc, "proj")
     assert abs(val - 0.88528925443) < 1e-12
+
+
+@pytest.mark.parametrize("elem,expected", [
+    # test/stokes3dhex.cpp:135-140 (checkError, absolute 1e-12)
+    ("hex", [1.309442419567852e-15, 1.021847252919293e-14, 1.800953966048908e-15, 1.097009563518918e-14]),
+    # test/stokes3dtet.cpp:122-127
+    ("tet", [1.191610761242353e-15, 4.347071660478249e-15, 1.168951507916659e-15, 5.36156027085171e-14]),
+])
+def test_oracle_stokes_goldens(elem, expected):
+    """Vector spaces (BLOCK ordering), tensor stiffness and the grad / div couplings of
+    the oracle, through proxpde's Taylor-Hood Stokes tests: Poiseuille flow in the box
+    [0,1] x [0,2] x [0,1], 4^3 cells, with the tests' six BCEss (component lists)."""
+    err, _, _ = O.stokes_golden(elem)
+    for e, r in zip(err, expected):
+        assert abs(e - r) < 1e-12
