@@ -28,6 +28,7 @@ __all__ = [
     "Tetrahedron", "Hexahedron", "Mesh", "buildHyperCube", "FESpace", "BCEss", "side", "Builder",
     "AssemblyStiffness", "AssemblyStiffnessFE", "AssemblyScalarMass", "AssemblyMass", "AssemblyRhsAnalytic",
     "AssemblyS2SProjection", "AssemblyProjection", "interpolateAnalyticFunction", "Context", "PxgError",
+    "AssemblyTensorStiffness", "AssemblyGrad", "AssemblyDiv",
     "FN_CONST", "FN_SIN3", "FN_POISSON_RHS", "FN_POISSON_EXACT", "P1TET", "P2TET", "Q1HEX", "Q2HEX", "meshgen",
     "load", "SCATTER_REDUCE", "SCATTER_COLOUR",
 ]
@@ -59,13 +60,14 @@ class Mesh:
         self.facets = facets
 
 
-def buildHyperCube(elem, n: int) -> Mesh:
-    """buildCube on [0,1]^3 with n^3 cubes (src/mesh.cpp:355-534): hexahedra, or 5
-    tetrahedra per cube."""
+def buildHyperCube(elem, n: int, origin=(0.0, 0.0, 0.0), length=(1.0, 1.0, 1.0)) -> Mesh:
+    """buildCube on the box origin + [0, length] with n^3 cells (src/mesh.cpp:355-534):
+    hexahedra, or 5 tetrahedra per cell."""
     if elem is Hexahedron:
         xyz, conn = meshgen.cube_hex(n)
     else:
         xyz, conn = meshgen.cube_tet5(n)
+    xyz = np.asarray(origin, dtype=np.float64) + xyz * np.asarray(length, dtype=np.float64)
     m = Mesh(elem, xyz, conn)
     m.structured_n = n
     return m
@@ -97,10 +99,16 @@ class FESpace:
     """FESpace<Mesh, LagrangeFE<Elem, order>::RefFE_T, RecommendedQR>: owns the device
     context with the mesh, the first-touch DOF map and the CSR pattern."""
 
-    def __init__(self, mesh: Mesh, order: int = 1, device: int = 0, elem_map=None, ndof=None):
+    def __init__(self, mesh: Mesh, order: int = 1, device: int = 0, elem_map=None, ndof=None, dim: int = 1,
+                 offset: int = 0, qr_order=None):
         self.mesh = mesh
         self.order = order
         self.etype = _etype(mesh.elem, order)
+        # vector spaces (BLOCK ordering), the offset in a global system and the element
+        # type whose quadrature rule the space uses (FESpace<Mesh, RefFE, QR, dim>)
+        self.dim = int(dim)
+        self.offset = int(offset)
+        self.qr_type = _etype(mesh.elem, qr_order or order)
         self.ctx = Context(device)
         self.ctx.set_mesh(self.etype, mesh.xyz, mesh.conn)
         if elem_map is None:
@@ -153,7 +161,7 @@ class FESpace:
             return
         if not bcs:
             self.ctx.set_bc(np.zeros(0, np.uint32), np.zeros(0), 1.0)
-        elif all(b.marker is not None for b in bcs):
+        elif all(b.device_setup for b in bcs):
             # marked facets -> constrained DOFs on the device (BCEss::setupDofMap)
             self.mark_facets()
             self.ctx.set_bc_markers([(b.marker, FN_CONST, b.value) for b in bcs], bcs[-1].diag)
@@ -193,17 +201,22 @@ HEX_FACES = [[0, 3, 2, 1], [3, 0, 4, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6
 
 class BCEss:
     """Essential BC on the DOFs of the boundary facets with a marker (bc.hpp:252-295),
-    set up on the device from the facet markers; or on an explicit DOF list.  ``value``
-    is a constant (marker form) or an array per DOF (list form)."""
+    or on an explicit DOF list.  Marker form: ``value`` is a constant, or a function of
+    the DOF points (n x 3 array) returning n values (scalar space) or n x dim values
+    (vector space); ``comps`` restricts a vector BC to some components.  A scalar BC
+    with a constant is set up on the device from the facet markers; the others are
+    evaluated at the DOF points on the host (setup, off the assembly path)."""
 
-    def __init__(self, fe: FESpace, marker=None, value=0.0, dofs=None, diag=1.0):
+    def __init__(self, fe: FESpace, marker=None, value=0.0, dofs=None, diag=1.0, comps=None):
         self.fe = fe
         self.diag = float(diag)
         self._dofs = None
+        self.comps = list(range(fe.dim)) if comps is None else [int(c) for c in comps]
+        self.func = value if callable(value) else None
         if dofs is None:
-            if marker is None or np.ndim(value) != 0:
-                raise ValueError("BCEss: a marker with a constant value, or a DOF list")
-            self.marker, self.value = int(marker), float(value)
+            if marker is None or (self.func is None and np.ndim(value) != 0):
+                raise ValueError("BCEss: a marker with a constant or a function, or a DOF list")
+            self.marker, self.value = int(marker), (0.0 if self.func else float(value))
         else:
             self.marker = None
             self._dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
@@ -211,11 +224,30 @@ class BCEss:
             self.values = np.broadcast_to(v, self._dofs.shape).copy() if v.ndim == 0 else v.copy()
 
     @property
+    def device_setup(self):
+        """True when the constrained set is built on the device (scalar, constant)."""
+        return self.marker is not None and self.func is None and self.fe.dim == 1
+
+    def component_dofs(self):
+        """(component DOF ids k + c * ndof, values) over the space's component DOFs."""
+        if self.marker is None:
+            return self.dofs, self.values
+        ids = self._marker_dofs(self.fe, self.marker)
+        nd = self.fe.dof.size
+        if self.func is None:
+            vals = np.full((ids.size, self.fe.dim), self.value)
+        else:
+            pts = self.fe.dofPts()[ids]
+            vals = np.asarray(self.func(pts), dtype=np.float64).reshape(ids.size, -1)
+        out_d = np.concatenate([ids + c * nd for c in self.comps]).astype(np.uint32)
+        out_v = np.concatenate([vals[:, c if vals.shape[1] > 1 else 0] for c in self.comps])
+        return out_d, out_v
+
+    @property
     def dofs(self):
         """The constrained DOFs (host computation, for inspection)."""
         if self._dofs is None:
-            self._dofs = self._marker_dofs(self.fe, self.marker)
-            self.values = np.full(self._dofs.shape, self.value)
+            self._dofs, self.values = self.component_dofs()
         return self._dofs
 
     @staticmethod
@@ -232,10 +264,12 @@ class BCEss:
             node2dof = np.full(m.xyz.shape[0], -1, dtype=np.int64)
             node2dof[conn.reshape(-1).astype(np.int64)] = em[:, :nv].reshape(-1)
             return node2dof[sel]
-        # structured cube: the facets markFacetsCube tags with `marker` lie on one plane
-        axis, val = side.PLANE[marker]
+        # box: the facets markFacetsCube tags with `marker` lie on one plane of the box
+        axis, upper = side.PLANE[marker]
+        lo, hi = m.xyz[:, axis].min(), m.xyz[:, axis].max()
+        val = hi if upper else lo
         x = _interp_coord(fe, axis)
-        return np.nonzero(np.abs(x - val) <= 1e-6)[0]
+        return np.nonzero(np.abs(x - val) <= 1e-6 * (hi - lo))[0]
 
 
 # ----------------------------------------------------------------- assemblies
@@ -263,6 +297,39 @@ class AssemblyScalarMass:
 
 
 AssemblyMass = AssemblyScalarMass
+
+
+class AssemblyTensorStiffness:
+    """AssemblyTensorStiffness(c, feSpace) on a vector space (include/assembly_lhs.hpp:116-161)."""
+
+    def __init__(self, coef, fe):
+        self.fe, self.kind, self.coef = fe, 2, float(coef)
+
+
+class AssemblyGrad:
+    """AssemblyGrad(c, vector space, scalar space) (include/assembly_coupling.hpp:42-86)."""
+
+    def __init__(self, coef, fe1, fe2):
+        self.fe1, self.fe2, self.kind, self.coef = fe1, fe2, 4, float(coef)
+
+
+class AssemblyDiv:
+    """AssemblyDiv(c, scalar space, vector space) (include/assembly_coupling.hpp:89-132)."""
+
+    def __init__(self, coef, fe1, fe2):
+        self.fe1, self.fe2, self.kind, self.coef = fe1, fe2, 5, float(coef)
+
+
+def _sys_op(a):
+    """(space, kind, coef) of a square assembly in a system call."""
+    if getattr(a, "kind", None) == 2:
+        return a.fe, 2, a.coef
+    o = getattr(a, "op", None) or {}
+    if o.get("stiffness") == 1:
+        return a.fe, 1, o["stiff_coef"]
+    if o.get("mass") == 1:
+        return a.fe, 3, o["mass_coef"]
+    raise PxgError(6, f"{type(a).__name__} is not an assembly of the system path")
 
 
 class AssemblyRhsAnalytic:
@@ -300,9 +367,17 @@ class Builder:
     device value array on the structural pattern and into b; closeMatrix prunes
     |v| <= 1e-16 and exposes the CSR (A on the host as scipy, A_dev on the device)."""
 
-    def __init__(self, fe: FESpace):
+    def __init__(self, fe):
         import torch
 
+        if isinstance(fe, (int, np.integer)):
+            # Builder{numDOFs} over spaces with offsets: the calls are recorded and run on
+            # a device system (pxg_sys) by closeMatrix, when every space is known
+            self.size, self.fe, self._calls, self._rhs = int(fe), None, [], []
+            self.A = self.A_dev = None
+            self._b = None
+            return
+        self.size = None
         self.fe = fe
         self.dev = f"cuda:{fe.ctx.device}"
         fe.pattern()
@@ -311,7 +386,20 @@ class Builder:
         self.A = None
         self.A_dev = None
 
+    def buildCoupling(self, assembly, bcsRow=(), bcsCol=()):
+        """Builder::buildCoupling (include/builder.hpp:156-277)."""
+        if self.size is None:
+            raise PxgError(6, "buildCoupling needs Builder(numDOFs)")
+        self._calls.append((assembly.fe1, assembly.fe2, [(assembly.kind, assembly.coef)], list(bcsRow), list(bcsCol)))
+
     def buildLhs(self, assemblies, bcs=()):
+        if self.size is not None:
+            ops = [_sys_op(a) for a in assemblies]
+            fe = ops[0][0]
+            if any(o[0] is not fe for o in ops):
+                raise PxgError(6, "buildLhs: the assemblies of one call share one space")
+            self._calls.append((fe, fe, [(k, c) for _, k, c in ops], list(bcs), list(bcs)))
+            return
         op = {"stiffness": 0, "stiff_coef": 0.0, "mass": 0, "mass_coef": 0.0, "apply_bc": 1 if bcs else 0}
         if len(assemblies) == 0:
             raise ValueError("we need at least 1 assembly.")
@@ -331,16 +419,81 @@ class Builder:
         self.fe.ctx.assemble(op0=op, vals0=self.vals, b=self.b_dev if bcs else None, accumulate=True)
 
     def buildRhs(self, assemblies, bcs=()):
+        if self.size is not None:
+            if any(a.fe.dim != 1 for a in assemblies):
+                raise PxgError(6, "buildRhs on a vector space is not provided")
+            self._rhs.append((list(assemblies), list(bcs)))
+            return
         self.fe.apply_bcs(list(bcs))
         for a in assemblies:
             r = dict(a.rhs)
             r["apply_bc"] = 1 if bcs else 0
             self.fe.ctx.assemble(rhs=r, b=self.b_dev, accumulate=True)
 
+    def _close_system(self):
+        import scipy.sparse as sp
+        import torch
+
+        from ._lib import System
+
+        spaces = []
+        for fr, fc, _, _, _ in self._calls:
+            for f in (fr, fc):
+                if all(f is not g for g in spaces):
+                    spaces.append(f)
+        for a, _ in self._rhs:
+            for x in a:
+                if all(x.fe is not g for g in spaces):
+                    spaces.append(x.fe)
+        spaces.sort(key=lambda f: f.offset)
+        off = 0
+        for f in spaces:
+            if f.offset != off:
+                raise PxgError(1, f"space offsets: expected {off}, got {f.offset}")
+            off += f.dof.size * f.dim
+        if off != self.size:
+            raise PxgError(1, f"Builder size {self.size} != sum of the spaces' DOFs {off}")
+        S = System([f.ctx for f in spaces], [f.dim for f in spaces], [f.qr_type for f in spaces])
+        index = {id(f): k for k, f in enumerate(spaces)}
+        dev = f"cuda:{spaces[0].ctx.device}"
+        vals = torch.zeros(S.nnz, dtype=torch.float64, device=dev)
+        b = torch.zeros(S.ntot, dtype=torch.float64, device=dev)
+
+        def set_bcs(f, bcs):
+            if bcs:
+                d, v = zip(*(x.component_dofs() for x in bcs))
+                S.set_bc(index[id(f)], np.concatenate(d), np.concatenate(v), bcs[-1].diag)
+            else:
+                S.set_bc(index[id(f)], np.zeros(0, np.uint32), np.zeros(0))
+
+        for fr, fc, ops, br, bc in self._calls:
+            set_bcs(fr, br)
+            if fc is not fr:
+                set_bcs(fc, bc)
+            S.assemble(index[id(fr)], index[id(fc)], ops, vals, b, accumulate=True)
+        for assemblies, bcs in self._rhs:
+            for a in assemblies:
+                f = a.fe
+                f.apply_bcs(bcs)
+                r = dict(a.rhs)
+                r["apply_bc"] = 1 if bcs else 0
+                f.ctx.assemble(rhs=r, b=b[f.offset:f.offset + f.dof.size], accumulate=True)
+        rp, ci = S.get_pattern()
+        torch.cuda.synchronize()
+        A = sp.csr_matrix((vals.cpu().numpy(), ci, rp), shape=(S.ntot, S.ntot))
+        A.data[np.abs(A.data) <= 1e-16] = 0.0  # closeMatrix: prune(1, 1e-16)
+        A.eliminate_zeros()
+        A.sort_indices()
+        self.A = A
+        self._b = b
+        self._sys = S
+
     def closeMatrix(self):
         import scipy.sparse as sp
         import torch
 
+        if self.size is not None:
+            return self._close_system()
         ctx = self.fe.ctx
         rp_s, ci_s = ctx.pattern_device()
         n = self.fe.dof.size
@@ -367,6 +520,8 @@ class Builder:
         import torch
 
         torch.cuda.synchronize()
+        if self.size is not None:
+            return self._b.cpu().numpy() if self._b is not None else np.zeros(self.size)
         return self.b_dev.cpu().numpy()
 
     def clearRhs(self):

@@ -47,3 +47,43 @@ def test_golden_unstructured_p1(engine):
     d = np.load(os.path.join(GOLDEN, "cube_uns.npz"))
     mesh = px.Mesh(px.Tetrahedron, d["xyz"], d["tets"], facets=(d["tris"], d["tri_tags"]))
     assert abs(run(px, mesh, 1, "proj") - 0.88528925443) < 1e-12
+
+
+@pytest.mark.parametrize("elem,expected", [
+    # test/stokes3dhex.cpp:135-140
+    ("hex", [1.309442419567852e-15, 1.021847252919293e-14, 1.800953966048908e-15, 1.097009563518918e-14]),
+    # test/stokes3dtet.cpp:122-127
+    ("tet", [1.191610761242353e-15, 4.347071660478249e-15, 1.168951507916659e-15, 5.36156027085171e-14]),
+])
+def test_golden_stokes(engine, elem, expected):
+    """test/stokes3dhex.cpp and stokes3dtet.cpp written against the mirror: Taylor-Hood
+    spaces with offsets, Builder{numDOFs}, tensor stiffness, grad / div couplings and six
+    component-wise BCEss; solved on the host, error norms against the pinned values."""
+    px = engine
+    ly, nu = 2.0, 0.1
+    E = px.Hexahedron if elem == "hex" else px.Tetrahedron
+    mesh = px.buildHyperCube(E, 4, length=(1.0, ly, 1.0))
+    vel = px.FESpace(mesh, 2, dim=3)
+    p = px.FESpace(mesh, 1, offset=3 * vel.dof.size, qr_order=2)
+    inlet = lambda X: np.stack([0 * X[:, 0], 0.5 * (1.0 - X[:, 0] ** 2), 0 * X[:, 0]], axis=1)
+    zero = lambda X: np.zeros((X.shape[0], 3))
+    s = px.side
+    bcsVel = [px.BCEss(vel, s.BOTTOM, inlet), px.BCEss(vel, s.RIGHT, zero), px.BCEss(vel, s.TOP, zero, comps=[0, 2]),
+              px.BCEss(vel, s.LEFT, zero, comps=[0, 2]), px.BCEss(vel, s.BACK, zero, comps=[2]),
+              px.BCEss(vel, s.FRONT, zero, comps=[2])]
+    bcsP = []
+    n = 3 * vel.dof.size + p.dof.size
+    builder = px.Builder(n)
+    builder.buildLhs((px.AssemblyTensorStiffness(nu, vel),), bcsVel)
+    builder.buildCoupling(px.AssemblyGrad(-1.0, vel, p), bcsVel, bcsP)
+    builder.buildCoupling(px.AssemblyDiv(-1.0, p, vel), bcsP, bcsVel)
+    builder.closeMatrix()
+    sol = spla.spsolve(builder.A.tocsc(), builder.b)
+    nd = vel.dof.size
+    X = vel.dofPts()
+    ue = inlet(X)
+    pe = nu * (ly - p.dofPts()[:, 1])
+    err = [np.linalg.norm(sol[c * nd:(c + 1) * nd] - ue[:, c]) for c in range(3)]
+    err.append(np.linalg.norm(sol[3 * nd:] - pe))
+    for e, r in zip(err, expected):
+        assert abs(e - r) < 1e-12
