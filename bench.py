@@ -131,6 +131,60 @@ def cpu_sample(n_sample, threads):
     return conn.shape[0] / dt, dt
 
 
+def measure_widened(xyz, conn, n_stokes=16):
+    """The rows next to the assembly path: Dirichlet setup from facet markers on the
+    headline mesh (own context), and Taylor-Hood Stokes systems (vector space, tensor
+    stiffness, grad / div couplings) on n_stokes^3 boxes; device times of the calls."""
+    import torch
+
+    from proxpde_gb300 import _lib as L
+    from proxpde_gb300 import meshgen
+    from proxpde_gb300._lib import OP_DIV, OP_GRAD, OP_TENSOR_STIFFNESS, Context, System
+
+    out = {}
+    c = Context(0)
+    c.set_mesh(L.Q1HEX, xyz, conn)
+    c.build_dofmap()
+    t0 = time.perf_counter()
+    nf = c.build_facets()
+    t1 = time.perf_counter()
+    c.mark_facets_box()
+    t2 = time.perf_counter()
+    c.set_bc_markers([(m, L.FN_CONST, 0.0) for m in range(1, 7)])
+    t3 = time.perf_counter()
+    out["bc_setup_q1hex"] = {"elements": int(conn.shape[0]), "facets": nf, "build_facets_ms": 1e3 * (t1 - t0),
+                             "mark_box_ms": 1e3 * (t2 - t1), "set_bc_markers_ms": 1e3 * (t3 - t2)}
+    del c
+    for name, gen, tv, tp in (("stokes_q2q1_hex", meshgen.cube_hex, L.Q2HEX, L.Q1HEX),
+                              ("stokes_p2p1_tet", meshgen.cube_tet5, L.P2TET, L.P1TET)):
+        X, E = gen(n_stokes)
+        cv, cp = Context(0), Context(0)
+        cv.set_mesh(tv, X, E)
+        cp.set_mesh(tp, X, E)
+        cv.build_dofmap()
+        cp.build_dofmap()
+        S = System([cv, cp], [3, 1], qr_types=[tv, tv])
+        vals = torch.zeros(S.nnz, dtype=torch.float64, device="cuda")
+        b = torch.zeros(S.ntot, dtype=torch.float64, device="cuda")
+
+        def calls():
+            S.assemble(0, 0, [(OP_TENSOR_STIFFNESS, 0.1)], vals, b)
+            S.assemble(0, 1, [(OP_GRAD, -1.0)], vals, b, accumulate=True)
+            S.assemble(1, 0, [(OP_DIV, -1.0)], vals, b, accumulate=True)
+
+        calls()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(3):
+            calls()
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / 3
+        out[name] = {"n": n_stokes, "elements": int(E.shape[0]), "dofs": S.ntot, "nnz": S.nnz, "ms": ms,
+                     "elements_per_s": E.shape[0] / (ms * 1e-3)}
+    return out
+
+
 def measure_adjoint(n=96, reps=2):
     """Adjoint gradient dJ/dlog k_e on the perturbed Q1 96^3 cube (Dirichlet on all faces,
     f = 1, u_t = sin sin sin), device Jacobi-CG to 1e-10: forward + backward time."""
@@ -264,6 +318,7 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default kernels)")
+    ap.add_argument("--no-widened", action="store_true", help="skip the Dirichlet-setup and Stokes measurements")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-gradient measurement")
@@ -425,7 +480,9 @@ def main():
                "sample": f"{args.cpu_n}^3 Q1 hexes of the same workload (K+M+rhs), oracle restatement with OpenMP",
                "value_1thread": v_one, "sample_1thread": f"{min(args.cpu_n, 24)}^3 hexes, 1 thread"}
 
-    adjoint = batched = None
+    adjoint = batched = widened = None
+    if rank == 0 and not args.no_widened:
+        widened = measure_widened(xyz, conn)
     if rank == 0 and not args.no_adjoint:
         adjoint = measure_adjoint()
     if rank == 0 and not args.no_batched:
@@ -440,7 +497,7 @@ def main():
                        "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned), "tuning": tuning,
                        "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
                        "setup_s": setup_s, "parallelism": f"replicas x{world}"},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "widened": widened,
             "gpu_launches": 3 * args.steps, "adjoint": adjoint, "batched": batched,
         }
         print(json.dumps(line), flush=True)
