@@ -23,6 +23,7 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <stdexcept>
@@ -79,6 +80,17 @@ enum : int
   FRONT
 };
 } // namespace side
+
+// Point / vector value of the BC functions (the Vec3 of the reference's Fun<3, 3>)
+struct Vec3
+{
+  double v[3] = {0., 0., 0.};
+  Vec3() = default;
+  Vec3(double x, double y, double z): v{x, y, z} {}
+  double operator()(int i) const { return v[i]; }
+  double & operator()(int i) { return v[i]; }
+  static Vec3 Constant(double c) { return Vec3(c, c, c); }
+};
 
 template <typename Elem>
 struct Mesh
@@ -139,6 +151,17 @@ Mesh<Elem> buildHyperCube(int n)
   return m;
 }
 
+// buildHyperCube(mesh, origin, length, {n, n, n}) (include/mesh.hpp:385-421): the cube
+// above scaled to the box origin + [0, length]
+template <typename Elem>
+Mesh<Elem> buildHyperCube(std::array<double, 3> const & origin, std::array<double, 3> const & length, int n)
+{
+  Mesh<Elem> m = buildHyperCube<Elem>(n);
+  for (size_t k = 0; k < m.xyz.size(); ++k)
+    m.xyz[k] = origin[k % 3] + m.xyz[k] * length[k % 3];
+  return m;
+}
+
 // Device array owned through the C ABI.
 template <typename T>
 struct DeviceArray
@@ -183,19 +206,29 @@ struct DeviceArray
 
 // FESpace<Mesh, LagrangeFE<Elem, Order>::RefFE_T, RecommendedQR> on the device: the
 // mesh, the first-touch DOF map and the CSR pattern live in one engine context.
-template <typename Elem, int Order>
+// Dim components (BLOCK ordering) and the quadrature of order QrOrder make
+// FESpace<Mesh, RefFE, QR, Dim>; offset is the space's offset in a global system.
+template <typename Elem, int Order, int Dim = 1, int QrOrder = Order>
 struct FESpace
 {
-  static constexpr int elemType =
-      std::is_same_v<Elem, Tetrahedron> ? (Order == 1 ? PXG_P1TET : PXG_P2TET) : (Order == 1 ? PXG_Q1HEX : PXG_Q2HEX);
+  static constexpr int typeOf(int order)
+  {
+    return std::is_same_v<Elem, Tetrahedron> ? (order == 1 ? PXG_P1TET : PXG_P2TET)
+                                             : (order == 1 ? PXG_Q1HEX : PXG_Q2HEX);
+  }
+  static constexpr int elemType = typeOf(Order);
+  static constexpr int qrType = typeOf(QrOrder);
+  static constexpr int dim = Dim;
   pxg_ctx * ctx = nullptr;
   struct
   {
     int64_t size = 0;
   } dof;
   int64_t nnz = 0;
+  int64_t offset = 0;
+  double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.}; // bounding box of the mesh
 
-  explicit FESpace(Mesh<Elem> const & m, int device = 0)
+  explicit FESpace(Mesh<Elem> const & m, int64_t off = 0, int device = 0): offset(off)
   {
     check(pxg_create(&ctx, device), nullptr, "pxg_create");
     check(pxg_set_mesh(ctx, elemType, m.xyz.data(), m.nnodes(), m.conn.data(), m.nelem(), PXG_MEM_HOST), ctx,
@@ -204,7 +237,8 @@ struct FESpace
     check(pxg_build_pattern(ctx, &nnz), ctx, "pxg_build_pattern");
     // boundary facets marked on the planes of the bounding box, as markFacetsCube does
     // for buildHyperCube (include/mesh.hpp:443-481)
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int d = 0; d < 3; ++d)
+      lo[d] = 1e300, hi[d] = -1e300;
     for (size_t k = 0; k < m.xyz.size(); ++k)
     {
       lo[k % 3] = std::min(lo[k % 3], m.xyz[k]);
@@ -231,23 +265,67 @@ struct FESpace
   }
 };
 
-// BCEss{feSpace, marker, value} (include/bc.hpp:81-97): the DOFs of the boundary facets
-// with that marker, set up on the device (pxg_set_bc_markers); or an explicit DOF list.
+// BCEss (include/bc.hpp:81-97) on the DOFs of the boundary facets with a marker, or on
+// an explicit list.  Marker with a constant on a scalar space: the constrained set is
+// built on the device from the facet markers (pxg_set_bc_markers).  Marker with a
+// function of the point (scalar, or Vec3 on a vector space) and optional components:
+// evaluated at the DOF points on the host (setup, as the reference does).  `dofs` /
+// `values` always hold the constrained component DOFs (k + c * ndof) and their values,
+// which the system builder uses.
 struct BCEss
 {
-  int marker = side::NONE; // NONE: the explicit list below
+  int marker = side::NONE; // set: the scalar device path applies
   double value = 0.0;
   std::vector<uint32_t> dofs;
   std::vector<double> values;
   double diag = 1.0; // BCEss::diag (bc.hpp:301)
 
   template <typename FE>
-  BCEss(FE const &, int m, double v = 0.0): marker(m), value(v)
+  BCEss(FE const & fe, int m, double v = 0.0): value(v)
   {
     if (m < side::BOTTOM || m > side::FRONT)
       throw Error(PXG_ERR_INVALID_ARG, "BCEss: unknown side marker");
+    if constexpr (FE::dim == 1)
+      marker = m;
+    collect(fe, m, [v](Vec3 const &) { return Vec3::Constant(v); }, {});
+  }
+  template <typename FE, typename F, typename = std::enable_if_t<std::is_invocable_v<F const &, Vec3 const &>>>
+  BCEss(FE const & fe, int m, F const & fun, std::vector<int> comps = {})
+  {
+    if (m < side::BOTTOM || m > side::FRONT)
+      throw Error(PXG_ERR_INVALID_ARG, "BCEss: unknown side marker");
+    collect(fe, m, fun, comps);
   }
   BCEss(std::vector<uint32_t> d, std::vector<double> v): dofs(std::move(d)), values(std::move(v)) {}
+
+private:
+  // the DOFs on the marker's plane of the box (markFacetsCube), for every component
+  template <typename FE, typename F>
+  void collect(FE const & fe, int m, F const & fun, std::vector<int> comps)
+  {
+    int const axis = (m == side::RIGHT || m == side::LEFT) ? 0 : (m == side::BOTTOM || m == side::TOP) ? 1 : 2;
+    bool const upper = m == side::RIGHT || m == side::TOP || m == side::FRONT;
+    double const plane = upper ? fe.hi[axis] : fe.lo[axis], tol = 1e-6 * (fe.hi[axis] - fe.lo[axis]);
+    std::vector<double> const x = fe.interpolate(PXG_FN_COORD_X), y = fe.interpolate(PXG_FN_COORD_Y),
+                              z = fe.interpolate(PXG_FN_COORD_Z);
+    if (comps.empty())
+      for (int c = 0; c < FE::dim; ++c)
+        comps.push_back(c);
+    std::vector<double> const & xa = axis == 0 ? x : axis == 1 ? y : z;
+    for (int c: comps)
+      for (size_t k = 0; k < xa.size(); ++k)
+        if (std::fabs(xa[k] - plane) <= tol)
+        {
+          auto const r = fun(Vec3(x[k], y[k], z[k]));
+          double val;
+          if constexpr (std::is_arithmetic_v<std::decay_t<decltype(r)>>)
+            val = r;
+          else
+            val = r(c);
+          dofs.push_back((uint32_t)(k + (size_t)c * xa.size()));
+          values.push_back(val);
+        }
+  }
 };
 
 // ------------------------------------------------------------------ assemblies
@@ -294,6 +372,36 @@ struct AssemblyProjection
   std::vector<double> const * field;
   FE const * feSpace;
   AssemblyProjection(double c, std::vector<double> const & r, FE const & fe): coef(c), field(&r), feSpace(&fe) {}
+};
+
+template <typename FE>
+struct AssemblyTensorStiffness
+{
+  double coef;
+  FE const * feSpace;
+  AssemblyTensorStiffness(double c, FE const & fe): coef(c), feSpace(&fe) {}
+};
+
+// AssemblyGrad(c, vector space, scalar space) (include/assembly_coupling.hpp:42-86)
+template <typename FE1, typename FE2>
+struct AssemblyGrad
+{
+  double coef;
+  FE1 const * feSpace1;
+  FE2 const * feSpace2;
+  AssemblyGrad(double c, FE1 const & a, FE2 const & b): coef(c), feSpace1(&a), feSpace2(&b) {}
+  static constexpr int kind = PXG_OP_GRAD;
+};
+
+// AssemblyDiv(c, scalar space, vector space) (include/assembly_coupling.hpp:89-132)
+template <typename FE1, typename FE2>
+struct AssemblyDiv
+{
+  double coef;
+  FE1 const * feSpace1;
+  FE2 const * feSpace2;
+  AssemblyDiv(double c, FE1 const & a, FE2 const & b): coef(c), feSpace1(&a), feSpace2(&b) {}
+  static constexpr int kind = PXG_OP_DIV;
 };
 
 // CSR matrix on the host
@@ -381,9 +489,7 @@ private:
       nm += bc.marker != side::NONE;
       diag = bc.diag;
     }
-    if (nm && nm != bcs.size())
-      throw Error(PXG_ERR_UNSUPPORTED, "BCEss: marker and DOF-list conditions in one call");
-    if (nm)
+    if (nm && nm == bcs.size())
     {
       // on the device: the marked facets' DOFs, constant values (later ones win)
       std::vector<int32_t> m, f;
@@ -447,7 +553,178 @@ private:
   }
 };
 
-template <typename FE>
+template <typename FE, std::enable_if_t<!std::is_arithmetic_v<std::remove_cv_t<FE>>, int> = 0>
 Builder(FE &) -> Builder<FE, StorageType::ClmMajor>;
+
+// Builder{numDOFs} over spaces with offsets (vector spaces, buildCoupling): the calls
+// are recorded and run on a device system (pxg_sys) by closeMatrix, when all the
+// spaces are known.
+template <StorageType Storage>
+struct Builder<void, Storage>
+{
+  int64_t size;
+  CsrMatrix A;
+  std::vector<double> b;
+
+  explicit Builder(int64_t n): size(n), b((size_t)n, 0.0) {}
+
+  template <typename... Asm>
+  void buildLhs(std::tuple<Asm...> const & assemblies, std::vector<BCEss> const & bcs = {})
+  {
+    static_assert(sizeof...(Asm) > 0, "we need at least 1 assembly.");
+    Call c;
+    std::apply([&](auto const &... a) { (addSquare(c, a), ...); }, assemblies);
+    c.col = c.row;
+    c.bcRow = c.bcCol = bcs;
+    calls.push_back(std::move(c));
+  }
+
+  template <typename Asm>
+  void buildCoupling(Asm const & a, std::vector<BCEss> const & bcsRow, std::vector<BCEss> const & bcsCol)
+  {
+    Call c;
+    c.row = spaceOf(*a.feSpace1);
+    c.col = spaceOf(*a.feSpace2);
+    c.kinds.push_back(Asm::kind);
+    c.coefs.push_back(a.coef);
+    c.bcRow = bcsRow;
+    c.bcCol = bcsCol;
+    calls.push_back(std::move(c));
+  }
+
+  // setFromTriplets + prune(1., 1e-16) (builder.hpp:366-371) over the recorded calls
+  void closeMatrix()
+  {
+    std::vector<int> order(spaces.size());
+    for (size_t k = 0; k < order.size(); ++k)
+      order[k] = (int)k;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return spaces[x].offset < spaces[y].offset; });
+    std::vector<pxg_ctx *> ctxs;
+    std::vector<int> dims, qrs, slot(spaces.size());
+    int64_t off = 0;
+    for (size_t k = 0; k < order.size(); ++k)
+    {
+      Space const & sp = spaces[order[k]];
+      if (sp.offset != off)
+        throw Error(PXG_ERR_INVALID_ARG, "Builder: the spaces' offsets do not tile the system");
+      off += sp.ndof * sp.dim;
+      ctxs.push_back(sp.ctx);
+      dims.push_back(sp.dim);
+      qrs.push_back(sp.qr);
+      slot[order[k]] = (int)k;
+    }
+    if (off != size)
+      throw Error(PXG_ERR_INVALID_ARG, "Builder: size differs from the spaces' DOFs");
+    pxg_ctx * c0 = ctxs[0];
+    pxg_sys * S = nullptr;
+    int64_t ntot = 0, nnz = 0;
+    check(pxg_sys_create(&S, ctxs.data(), dims.data(), qrs.data(), (int)ctxs.size(), &ntot, &nnz), c0,
+          "pxg_sys_create");
+    struct Guard
+    {
+      pxg_sys * s;
+      ~Guard() { pxg_sys_destroy(s); }
+    } guard{S};
+    DeviceArray<double> vals(c0, (size_t)nnz), bd(c0, (size_t)ntot);
+    vals.zero();
+    bd.zero();
+    auto setBcs = [&](int s, std::vector<BCEss> const & bcs) {
+      std::vector<uint32_t> d;
+      std::vector<double> v;
+      double diag = 1.0;
+      for (auto const & bc: bcs)
+      {
+        d.insert(d.end(), bc.dofs.begin(), bc.dofs.end());
+        v.insert(v.end(), bc.values.begin(), bc.values.end());
+        diag = bc.diag;
+      }
+      check(pxg_sys_set_bc(S, s, d.data(), v.data(), (int64_t)d.size(), diag), c0, "pxg_sys_set_bc");
+    };
+    for (auto const & c: calls)
+    {
+      setBcs(slot[c.row], c.bcRow);
+      if (c.col != c.row)
+        setBcs(slot[c.col], c.bcCol);
+      check(pxg_sys_assemble(S, slot[c.row], slot[c.col], c.kinds.data(), c.coefs.data(), (int)c.kinds.size(),
+                             vals.p, bd.p, PXG_ACCUMULATE, nullptr),
+            c0, "pxg_sys_assemble");
+    }
+    int32_t const * rp = nullptr;
+    int32_t const * ci = nullptr;
+    check(pxg_sys_pattern_device(S, &rp, &ci), c0, "pxg_sys_pattern_device");
+    DeviceArray<int32_t> rpo(c0, (size_t)ntot + 1), cio(c0, (size_t)nnz);
+    DeviceArray<double> vo(c0, (size_t)nnz);
+    int64_t kept = 0;
+    check(pxg_prune_csr_noalloc(rp, ci, vals.p, ntot, rpo.p, cio.p, vo.p, &kept, nullptr), c0,
+          "pxg_prune_csr_noalloc");
+    A.rows = A.cols = ntot;
+    A.outer = rpo.host();
+    A.inner = cio.host();
+    A.inner.resize((size_t)kept);
+    A.values = vo.host();
+    A.values.resize((size_t)kept);
+    b = bd.host();
+    calls.clear(); // the triplets were consumed (builder.hpp:370)
+  }
+
+private:
+  struct Space
+  {
+    pxg_ctx * ctx;
+    int dim, qr;
+    int64_t offset, ndof;
+  };
+  struct Call
+  {
+    int row = -1, col = -1;
+    std::vector<int> kinds;
+    std::vector<double> coefs;
+    std::vector<BCEss> bcRow, bcCol;
+  };
+  std::vector<Space> spaces;
+  std::vector<Call> calls;
+
+  template <typename FE>
+  int spaceOf(FE const & fe)
+  {
+    for (size_t k = 0; k < spaces.size(); ++k)
+      if (spaces[k].ctx == fe.ctx)
+        return (int)k;
+    spaces.push_back(Space{fe.ctx, FE::dim, FE::qrType, fe.offset, fe.dof.size});
+    return (int)spaces.size() - 1;
+  }
+  template <typename FE>
+  void setRow(Call & c, FE const & fe)
+  {
+    int const s = spaceOf(fe);
+    if (c.row >= 0 && c.row != s)
+      throw Error(PXG_ERR_INVALID_ARG, "buildLhs: the assemblies of one call share one space");
+    c.row = s;
+  }
+  template <typename X>
+  void addSquare(Call & c, AssemblyStiffness<X> const & a)
+  {
+    setRow(c, *a.feSpace);
+    c.kinds.push_back(PXG_OP_STIFFNESS);
+    c.coefs.push_back(a.coef);
+  }
+  template <typename X>
+  void addSquare(Call & c, AssemblyTensorStiffness<X> const & a)
+  {
+    setRow(c, *a.feSpace);
+    c.kinds.push_back(PXG_OP_TENSOR_STIFFNESS);
+    c.coefs.push_back(a.coef);
+  }
+  template <typename X>
+  void addSquare(Call & c, AssemblyScalarMass<X> const & a)
+  {
+    setRow(c, *a.feSpace);
+    c.kinds.push_back(PXG_OP_MASS);
+    c.coefs.push_back(a.coef);
+  }
+};
+
+template <typename I, std::enable_if_t<std::is_integral_v<I>, int> = 0>
+Builder(I) -> Builder<void, StorageType::ClmMajor>;
 
 } // namespace proxgpu

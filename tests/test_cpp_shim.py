@@ -11,9 +11,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "poisson3d.cpp")
 
 
-def test_shim_compiles(tmp_path):
+STOKES = os.path.join(ROOT, "tests", "cpp", "stokes3d.cpp")
+
+
+@pytest.mark.parametrize("src", [SRC, STOKES], ids=["poisson3d", "stokes3d"])
+def test_shim_compiles(tmp_path, src):
     r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
-                        SRC], capture_output=True, text=True)
+                        src], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
 
@@ -47,3 +51,42 @@ def test_shim_reproduces_goldens(engine, tmp_path, order, n, expected):
     A = sp.csr_matrix((va, ci, rp), shape=(nrow, nrow)).tocsc()
     u = spla.spsolve(A, b)
     assert abs(np.linalg.norm(u - ex) - expected) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("elem,expected", [
+    # test/stokes3dhex.cpp:135-140
+    ("hex", [1.309442419567852e-15, 1.021847252919293e-14, 1.800953966048908e-15, 1.097009563518918e-14]),
+    # test/stokes3dtet.cpp:122-127
+    ("tet", [1.191610761242353e-15, 4.347071660478249e-15, 1.168951507916659e-15, 5.36156027085171e-14]),
+])
+def test_shim_stokes_goldens(engine, tmp_path, elem, expected):
+    """The C++ port of proxpde's Stokes tests on the shim (vector space, Builder{numDOFs},
+    buildCoupling, component-wise BCEss with functions) reproduces their error norms."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    from proxpde_gb300 import build
+
+    lib = build.build()
+    exe = tmp_path / "stokes3d"
+    r = subprocess.run(["g++", "-std=c++20", "-O2", "-I", os.path.join(ROOT, "include"), STOKES, "-o", str(exe),
+                        f"-L{os.path.dirname(lib)}", "-lpxg", f"-Wl,-rpath,{os.path.dirname(lib)}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), elem, str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = out.read_bytes()
+    nrow, nnz, ndu = np.frombuffer(raw[:24], dtype=np.int64)
+    off = 24
+    rp = np.frombuffer(raw, np.int32, nrow + 1, off); off += 4 * (nrow + 1)
+    ci = np.frombuffer(raw, np.int32, nnz, off); off += 4 * nnz
+    va = np.frombuffer(raw, np.float64, nnz, off); off += 8 * nnz
+    b = np.frombuffer(raw, np.float64, nrow, off); off += 8 * nrow
+    ex = np.frombuffer(raw, np.float64, nrow, off)
+    u = spla.spsolve(sp.csr_matrix((va, ci, rp), shape=(nrow, nrow)).tocsc(), b)
+    err = [np.linalg.norm(u[c * ndu:(c + 1) * ndu] - ex[c * ndu:(c + 1) * ndu]) for c in range(3)]
+    err.append(np.linalg.norm(u[3 * ndu:] - ex[3 * ndu:]))
+    for e, r_ in zip(err, expected):
+        assert abs(e - r_) < 1e-12
