@@ -280,6 +280,18 @@ def dist_init(args):
     return world, rank, local
 
 
+def max_over_ranks(x, world, device):
+    """The job's time: the largest of the ranks' values (no-op on one rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -327,7 +339,12 @@ def main():
 
     world, rank, local = dist_init(args)
     if args.impl == "reference":
+        # the CPU reference arm: rank 0 times the oracle, the other ranks exit
         run_reference(args, world, rank)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
         return
 
     import torch
@@ -394,13 +411,7 @@ def main():
     torch.cuda.synchronize()
     pruned = cnt.tolist()
     clocks = clk.stop()
-    total_ms = start.elapsed_time(stop)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = t.item()
+    total_ms = max_over_ranks(start.elapsed_time(stop), world, dev)
     ms_step = total_ms / args.steps
     asm_ms = statistics.mean(a.elapsed_time(c) for a, c in ev)
     value = world * E / (ms_step * 1e-3)
