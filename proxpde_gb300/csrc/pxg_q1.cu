@@ -967,11 +967,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
         R[qw] = dot2(x0, s0, x1, s1);
       }
       // classes along w
-      T const sum = R[0] + R[1], dif = R[0] - R[1];
-      T const as = cst<T>(kAlpha01) * sum, bd = cst<T>(kBeta0) * dif;
-      sh.u.tab[l * 12 + r * 3 + 0] = as + bd;
-      sh.u.tab[l * 12 + r * 3 + 1] = as - bd;
-      sh.u.tab[l * 12 + r * 3 + 2] = cst<T>(AB) * sum;
+      sh.u.tab[l * 12 + r * 3 + 0] = dot2(cst<T>(AA), R[0], cst<T>(BB), R[1]);
+      sh.u.tab[l * 12 + r * 3 + 1] = dot2(cst<T>(BB), R[0], cst<T>(AA), R[1]);
+      sh.u.tab[l * 12 + r * 3 + 2] = cst<T>(AB) * (R[0] + R[1]);
     }
   }
   __syncthreads();
@@ -980,13 +978,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
   bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
   double const kfac = a.kE ? a.kE[e] : 1.0;
-  T ks[2], ms[2];
+  // operator coefficients, applied in FP64 to the converted entry values (the FP64
+  // pipe has room; a double-float product and a conversion per operator cost more)
+  double ks[2], ms[2];
 #pragma unroll
   for (int m = 0; m < 2; ++m)
   {
     LhsDev const & op = a.op[m];
-    ks[m] = fromDouble<T>(op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.);
-    ms[m] = fromDouble<T>(op.mass ? op.mc : 0.);
+    ks[m] = op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.;
+    ms[m] = op.mass ? op.mc : 0.;
   }
   T const * tb = sh.u.tab;
   for (int k = 0; k < 5; ++k)
@@ -1018,6 +1018,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       T const beta = negIf(cx == 2 ? cst<T>(0.0) : cst<T>(kBeta0), cx == 1);
       mv = dot2(alpha, tb[mo], beta, tb[mo + 12]);
     }
+    double const kd = needK ? toDouble(kv) : 0., md = needM ? toDouble(mv) : 0.;
     bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
 #pragma unroll
     for (int m = 0; m < 2; ++m)
@@ -1025,8 +1026,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       LhsDev const & op = a.op[m];
       if (!op.on)
         continue;
-      T const v = op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv;
-      double const val = toDouble(v);
+      double const val = op.stiff ? (op.mass ? fma(ks[m], kd, ms[m] * md) : ks[m] * kd) : ms[m] * md;
       if (!live)
         continue;
       if (anyBc && op.bc && (ci || cj))
