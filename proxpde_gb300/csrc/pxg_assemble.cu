@@ -800,7 +800,7 @@ void threadCandidates(pxg_ctx const * c, int (&out)[4])
   if (c->etype == P1TET || c->etype == P2TET)
     out[0] = 64, out[1] = 128, out[2] = 256;
   else if (c->etype == Q1HEX && !c->q1Generic && !c->q1Thread)
-    out[0] = 128, out[1] = 256, out[2] = 512;
+    out[0] = 256, out[1] = 512;
   else
     out[0] = 128;
 }

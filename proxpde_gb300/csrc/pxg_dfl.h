@@ -127,6 +127,26 @@ __device__ __forceinline__ double sumStart(double t) { return t; }
 __device__ __forceinline__ void sumAdd(double & a, double t) { a += t; }
 __device__ __forceinline__ double sumEnd(double a) { return a; }
 
+// The same with a sign on each term, given as the bits of the float +1 or -1: the
+// products with +-1 are exact, so that the FMAs below round like the additions of
+// sumAdd on the negated term, and the sign costs no instruction.
+__device__ __forceinline__ DflSum sumStartS(dfl t, uint32_t sg)
+{
+  float const f = __uint_as_float(sg);
+  return DflSum{__fmul_rn(f, t.h), __fmul_rn(f, t.l)};
+}
+__device__ __forceinline__ void sumAddS(DflSum & a, dfl t, uint32_t sg)
+{
+  float const f = __uint_as_float(sg);
+  float const s = __fmaf_rn(f, t.h, a.s);
+  float const bb = __fsub_rn(s, a.s);
+  float const e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fmaf_rn(f, t.h, -bb));
+  a.s = s;
+  a.c = __fadd_rn(a.c, __fmaf_rn(f, t.l, e));
+}
+__device__ __forceinline__ double sumStartS(double t, uint32_t sg) { return (sg >> 31) ? -t : t; }
+__device__ __forceinline__ void sumAddS(double & a, double t, uint32_t sg) { a += (sg >> 31) ? -t : t; }
+
 // 1/a: float reciprocal refined by one Newton step in double-float
 __device__ __forceinline__ dfl rcp(dfl a)
 {

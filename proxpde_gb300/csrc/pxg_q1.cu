@@ -590,26 +590,6 @@ constexpr int kThreads = 256;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kAlpha01 = 0.5 * (AA + BB), kBeta0 = 0.5 * (AA - BB);
 
-template <typename T>
-struct __align__(16) ElemShared
-{
-  union
-  {
-    T G[7][8];     // A -> B: G_xx, G_yy, G_zz, G_xy, G_xz, G_yz and |det J| per Gauss point
-    T tab[8 * 12]; // B -> C: tables, [job * 12 + row * 3 + class]
-  } u;
-  double bv[8];      // Dirichlet value of each node (0 when free)
-  int32_t rp[8];     // rowPtr of each node's DOF
-  uint32_t dof[8];
-  uint16_t rank[64]; // scatter ranks of the element's 8 x 8 entries
-  uint32_t pad[16];  // slot stride 1088 B: the four groups of a warp start 16 banks apart
-};
-template <int NT>
-constexpr size_t smemBytes()
-{
-  return (NT / 8) * sizeof(ElemShared<dfl>) + 36 * sizeof(uint4);
-}
-
 __device__ __forceinline__ dfl shx(dfl v, int m)
 {
   return dfl{__shfl_xor_sync(kFull, v.h, m), __shfl_xor_sync(kFull, v.l, m)};
@@ -692,38 +672,81 @@ constexpr uint64_t kJobsLo = jobc(0, 0, 1, 2, 0) | jobc(1, 1, 0, 2, 0) << 16 | j
 constexpr uint64_t kJobsHi = jobc(6, 0, 1, 2, 1) | jobc(3, 0, 1, 2, 2) << 16 | jobc(4, 0, 2, 1, 2) << 32 |
                              jobc(5, 1, 2, 0, 2) << 48;
 
-// Entry p of the 36 pairs i <= j (row-major): the table offsets of the nine stiffness
-// terms (the formulas of q1Stiffness), their signs, the mass-table offset and cx.
-__device__ uint4 pairDesc(int p)
+// Shared memory of a block of NT threads, NS = NT / 8 element slots (one per lane group):
+//   tab   T[96][NS + 1]: the tables (phase B -> C), row job * 12 + row * 3 + class,
+//         one column per slot; it aliases G, T[NS][kGStride] (phase A -> B), where a
+//         slot holds G_xx, G_yy, G_zz, G_xy, G_xz, G_yz and |det J| at its 8 Gauss points
+//   slotw uint32_t[NS][kSlotWords]: rowPtr of the nodes' DOFs, the DOFs, the 8 x 8
+//         scatter ranks (uint16) and the mask of constrained nodes
+//   bv    double[NS][kBvStride]: Dirichlet value of each node (0 when free)
+// The slot strides are odd multiples of the access width, so that the lane-per-slot
+// reads of phase C, and the group-per-slot accesses of the other phases, spread over
+// the banks.
+constexpr int kGStride = 57, kSlotWords = 49, kBvStride = 9;
+constexpr int kSwRp = 0, kSwDof = 8, kSwRank = 16, kSwCons = 48;
+
+template <int NT>
+struct Smem
 {
-  int i = 0;
-  while (p >= 8 - i)
-  {
-    p -= 8 - i;
-    ++i;
-  }
-  int const j = i + p;
-  int const li = i ^ ((i >> 1) & 1), lj = j ^ ((j >> 1) & 1);
-  int const ix = li & 1, iy = (li >> 1) & 1, iz = li >> 2;
-  int const jx = lj & 1, jy = (lj >> 1) & 1, jz = lj >> 2;
-  int const cx = cls(ix, jx), cy = cls(iy, jy), cz = cls(iz, jz);
-  uint32_t const off[9] = {
-      (uint32_t)(0 * 12 + cy * 3 + cz),            (uint32_t)(1 * 12 + cx * 3 + cz),
-      (uint32_t)(2 * 12 + cx * 3 + cy),            (uint32_t)(5 * 12 + (2 * jx + iy) * 3 + cz),
-      (uint32_t)(5 * 12 + (2 * ix + jy) * 3 + cz), (uint32_t)(6 * 12 + (2 * jx + iz) * 3 + cy),
-      (uint32_t)(6 * 12 + (2 * ix + jz) * 3 + cy), (uint32_t)(7 * 12 + (2 * jy + iz) * 3 + cx),
-      (uint32_t)(7 * 12 + (2 * iy + jz) * 3 + cx)};
-  bool const pos[9] = {ix == jx, iy == jy, iz == jz, ix == jy, iy == jx, ix == jz, iz == jx, iy == jz, iz == jy};
-  uint32_t neg = 0;
-  for (int k = 0; k < 9; ++k)
-    neg |= pos[k] ? 0u : 1u << k;
-  uint4 d;
-  d.x = (uint32_t)i | (uint32_t)j << 3 | (uint32_t)cx << 6 | neg << 8;
-  d.y = off[0] | off[1] << 8 | off[2] << 16 | off[3] << 24;
-  d.z = off[4] | off[5] << 8 | off[6] << 16 | off[7] << 24;
-  d.w = off[8] | (uint32_t)(3 * 12 + cy * 3 + cz) << 8;
-  return d;
+  static constexpr int NS = NT / 8, kRow = NS + 1;
+  static constexpr size_t tabBytes = (size_t)(96 * kRow > NS * kGStride ? 96 * kRow : NS * kGStride) * 8;
+  static constexpr size_t slotOff = (tabBytes + 15) / 16 * 16;
+  static constexpr size_t bvOff = slotOff + ((size_t)NS * kSlotWords * 4 + 15) / 16 * 16;
+  static constexpr size_t bytes = bvOff + (size_t)NS * kBvStride * 8;
+};
+template <int NT>
+constexpr size_t smemBytes()
+{
+  return Smem<NT>::bytes;
 }
+
+// The 36 pairs i <= j (row-major) as 24 words each, read by a whole warp at once:
+//   [0..8]   byte offsets in a slot's column of tab of the nine stiffness terms (the
+//            formulas of q1Stiffness), [9..17] their signs as floats +-1,
+//   [18, 19] byte offsets of the two mass-table terms, [20] cx (the class of the pair
+//            along x), [21] i | j << 3, [22] the byte offsets in the rank array of
+//            entries (i, j) and (j, i), low and high half, [23] unused.
+template <int NS>
+struct PairTable
+{
+  alignas(16) uint32_t w[36 * 24];
+};
+template <int NS>
+constexpr PairTable<NS> makePairTable()
+{
+  PairTable<NS> t{};
+  constexpr uint32_t row = 8u * (NS + 1);
+  int p = 0;
+  for (int i = 0; i < 8; ++i)
+    for (int j = i; j < 8; ++j, ++p)
+    {
+      int const li = i ^ ((i >> 1) & 1), lj = j ^ ((j >> 1) & 1);
+      int const ix = li & 1, iy = (li >> 1) & 1, iz = li >> 2;
+      int const jx = lj & 1, jy = (lj >> 1) & 1, jz = lj >> 2;
+      int const cx = cls(ix, jx), cy = cls(iy, jy), cz = cls(iz, jz);
+      uint32_t const off[9] = {(uint32_t)(0 * 12 + cy * 3 + cz),            (uint32_t)(1 * 12 + cx * 3 + cz),
+                               (uint32_t)(2 * 12 + cx * 3 + cy),            (uint32_t)(5 * 12 + (2 * jx + iy) * 3 + cz),
+                               (uint32_t)(5 * 12 + (2 * ix + jy) * 3 + cz), (uint32_t)(6 * 12 + (2 * jx + iz) * 3 + cy),
+                               (uint32_t)(6 * 12 + (2 * ix + jz) * 3 + cy), (uint32_t)(7 * 12 + (2 * jy + iz) * 3 + cx),
+                               (uint32_t)(7 * 12 + (2 * iy + jz) * 3 + cx)};
+      bool const pos[9] = {ix == jx, iy == jy, iz == jz, ix == jy, iy == jx, ix == jz, iz == jx, iy == jz, iz == jy};
+      uint32_t * w = t.w + 24 * p;
+      for (int k = 0; k < 9; ++k)
+      {
+        w[k] = off[k] * row;
+        w[9 + k] = pos[k] ? 0x3f800000u : 0xbf800000u;
+      }
+      w[18] = (uint32_t)(3 * 12 + cy * 3 + cz) * row;
+      w[19] = (uint32_t)(4 * 12 + cy * 3 + cz) * row;
+      w[20] = (uint32_t)cx;
+      w[21] = (uint32_t)(i | j << 3);
+      w[22] = (uint32_t)(2 * (i * 8 + j)) | (uint32_t)(2 * (j * 8 + i)) << 16;
+      w[23] = 0;
+    }
+  return t;
+}
+__device__ PairTable<32> const kPairs32 = makePairTable<32>();
+__device__ PairTable<64> const kPairs64 = makePairTable<64>();
 
 // Dirichlet condensation of one entry (builder.hpp:76-124): a constrained diagonal
 // takes bcDiag, a free row the lift -K_ij h_j.  Out of line: its FP64 code would
@@ -758,20 +781,31 @@ __device__ __forceinline__ T pick3(T const (&v)[3], int d)
   return d == 0 ? v[0] : (d == 1 ? v[1] : v[2]);
 }
 
+template <typename T>
+__device__ __forceinline__ T ldTab(char const * col, uint32_t off)
+{
+  return *reinterpret_cast<T const *>(col + off);
+}
+
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
 {
-  extern __shared__ uint4 dynShared[]; // ElemShared<T>[NT / 8], then the 36 pair descriptors
-  ElemShared<T> * shAll = reinterpret_cast<ElemShared<T> *>(dynShared);
-  uint4 * sDesc = reinterpret_cast<uint4 *>(shAll + NT / 8);
-  if (threadIdx.x < 36)
-    sDesc[threadIdx.x] = pairDesc(threadIdx.x);
-  __syncthreads();
+  using S = Smem<NT>;
+  constexpr int NS = S::NS, kRow = S::kRow, SW = NS / 32;
+  static_assert(NS % 32 == 0, "phase C takes a warp of slots at a time");
+  extern __shared__ uint4 dynShared[];
+  char * const smem = reinterpret_cast<char *>(dynShared);
+  T * const tab = reinterpret_cast<T *>(smem);
+  uint32_t * const slotw = reinterpret_cast<uint32_t *>(smem + S::slotOff);
+  double * const bvAll = reinterpret_cast<double *>(smem + S::bvOff);
 
   int const l = threadIdx.x & 7;
   int const g0 = threadIdx.x & 24; // first lane of the group in the warp
-  ElemShared<T> & sh = shAll[threadIdx.x >> 3];
-  int64_t const eg = ((int64_t)blockIdx.x * NT + threadIdx.x) >> 3;
+  int const slot = threadIdx.x >> 3;
+  T * const G = tab + slot * kGStride; // G[c * 8 + q]
+  uint32_t * const sw = slotw + slot * kSlotWords;
+  double * const bv = bvAll + slot * kBvStride;
+  int64_t const eg = (int64_t)blockIdx.x * NS + slot;
   bool const live = eg < a.nelem;
   int64_t const e = elemOf(a, live ? eg : a.nelem - 1); // a tail group recomputes the last element, writes nothing
   int const bx = l & 1, by = (l >> 1) & 1, bz = l >> 2;
@@ -781,12 +815,19 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   uint32_t const dofl = a.emap[8 * e + l];
   bool const cl = a.bcMask && a.bcMask[dofl];
   uint32_t const cons = (__ballot_sync(kFull, cl) >> g0) & 0xffu;
-  sh.dof[l] = dofl;
-  sh.bv[l] = (cl && a.bcVal) ? a.bcVal[dofl] : 0.;
+  double const bvl = (cl && a.bcVal) ? a.bcVal[dofl] : 0.;
+  sw[kSwDof + l] = dofl;
+  bv[l] = bvl;
+  if (l == 0)
+    sw[kSwCons] = cons;
   if (lhs)
   {
-    sh.rp[l] = a.rowPtr[dofl];
-    reinterpret_cast<uint4 *>(sh.rank)[l] = reinterpret_cast<uint4 const *>(a.rank + 64 * e)[l];
+    sw[kSwRp + l] = a.rowPtr[dofl];
+    uint4 const r = reinterpret_cast<uint4 const *>(a.rank + 64 * e)[l];
+    sw[kSwRank + 4 * l + 0] = r.x;
+    sw[kSwRank + 4 * l + 1] = r.y;
+    sw[kSwRank + 4 * l + 2] = r.z;
+    sw[kSwRank + 4 * l + 3] = r.w;
   }
 
   // ---- vertex coordinates: lane l = lattice vertex l = node l ^ by, relative to vertex 0
@@ -846,13 +887,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
     T const det = dot3(J[0][0], C[0][0], J[0][1], C[1][0], J[0][2], C[2][0]);
     adet = fabs(det);
     T const s = cst<T>(0.25) * rcp(adet);
-    sh.u.G[0][l] = s * dot3(C[0][0], C[0][0], C[0][1], C[0][1], C[0][2], C[0][2]);
-    sh.u.G[1][l] = s * dot3(C[1][0], C[1][0], C[1][1], C[1][1], C[1][2], C[1][2]);
-    sh.u.G[2][l] = s * dot3(C[2][0], C[2][0], C[2][1], C[2][1], C[2][2], C[2][2]);
-    sh.u.G[3][l] = s * dot3(C[0][0], C[1][0], C[0][1], C[1][1], C[0][2], C[1][2]);
-    sh.u.G[4][l] = s * dot3(C[0][0], C[2][0], C[0][1], C[2][1], C[0][2], C[2][2]);
-    sh.u.G[5][l] = s * dot3(C[1][0], C[2][0], C[1][1], C[2][1], C[1][2], C[2][2]);
-    sh.u.G[6][l] = adet;
+    G[0 * 8 + l] = s * dot3(C[0][0], C[0][0], C[0][1], C[0][1], C[0][2], C[0][2]);
+    G[1 * 8 + l] = s * dot3(C[1][0], C[1][0], C[1][1], C[1][1], C[1][2], C[1][2]);
+    G[2 * 8 + l] = s * dot3(C[2][0], C[2][0], C[2][1], C[2][1], C[2][2], C[2][2]);
+    G[3 * 8 + l] = s * dot3(C[0][0], C[1][0], C[0][1], C[1][1], C[0][2], C[1][2]);
+    G[4 * 8 + l] = s * dot3(C[0][0], C[2][0], C[0][1], C[2][1], C[0][2], C[2][2]);
+    G[5 * 8 + l] = s * dot3(C[1][0], C[2][0], C[1][1], C[2][1], C[1][2], C[2][2]);
+    G[6 * 8 + l] = adet;
     T const xq = negIf(cst<T>(g), !bx), yq = negIf(cst<T>(g), !by), zq = negIf(cst<T>(g), !bz);
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -863,12 +904,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   bool const anyBc = cons && ((a.op[0].on && a.op[0].bc) || (a.op[1].on && a.op[1].bc));
   if (a.b)
   {
-    if (anyBc && live && cl && sh.bv[l] != 0.)
+    if (anyBc && live && cl && bvl != 0.)
     {
 #pragma unroll
       for (int m = 0; m < 2; ++m)
         if (a.op[m].on && a.op[m].bc)
-          atomicAdd(a.b + dofl, sh.bv[l]);
+          atomicAdd(a.b + dofl, bvl);
     }
     if (a.rkind)
     {
@@ -907,7 +948,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       else
       {
         // projection of a DOF field: node values -> Gauss point
-        T v = fromDouble<T>(a.field[sh.dof[l ^ by]]);
+        T v = fromDouble<T>(a.field[sw[kSwDof + (l ^ by)]]);
         v = lerp2(v, 1);
         v = lerp2(v, 2);
         v = lerp2(v, 4);
@@ -918,17 +959,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       F = lerp2(F, 4);
       int const n = l ^ by;
       if (live && !(a.rbc && ((cons >> n) & 1u)))
-        atomicAdd(a.b + sh.dof[n], toDouble(F));
+        atomicAdd(a.b + sw[kSwDof + n], toDouble(F));
     }
   }
   if (!lhs)
     return; // uniform over the block: the kernel arguments
 
   // ---- B. tables, lane l = job l
-  __syncthreads();
+  __syncthreads(); // G of every slot is written
   {
     uint32_t const code = (uint32_t)((l < 4 ? kJobsLo : kJobsHi) >> (16 * (l & 3))) & 0x7ffu;
-    int const cmp = code & 7, su = 1 << ((code >> 3) & 3), sv = 1 << ((code >> 5) & 3), sw = 1 << ((code >> 7) & 3);
+    int const cmp = code & 7, su = 1 << ((code >> 3) & 3), sv = 1 << ((code >> 5) & 3), sw3 = 1 << ((code >> 7) & 3);
     int const kind = code >> 9;
     T F[2][2][2]; // [qw][qv][qu]
 #pragma unroll
@@ -937,11 +978,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       for (int qv = 0; qv < 2; ++qv)
 #pragma unroll
         for (int qu = 0; qu < 2; ++qu)
-          F[qw][qv][qu] = sh.u.G[cmp][qu * su + qv * sv + qw * sw];
+          F[qw][qv][qu] = G[cmp * 8 + qu * su + qv * sv + qw * sw3];
     __syncthreads(); // the tables overwrite G
+    // constants of the class formulas, evaluated at compile time
+    constexpr T kOne = cst<T>(1.0), kMinusOne = cst<T>(-1.0), kZero = cst<T>(0.0);
+    constexpr T kA = cst<T>(A), kB = cst<T>(B), kAA = cst<T>(AA), kBB = cst<T>(BB), kAB = cst<T>(AB);
     bool const isU = kind == 2;
-    T const a0 = isU ? cst<T>(A) : cst<T>(1.0);
-    T const a1 = isU ? cst<T>(B) : (kind == 1 ? cst<T>(-1.0) : cst<T>(1.0));
+    T const a0 = isU ? kA : kOne;
+    T const a1 = isU ? kB : (kind == 1 ? kMinusOne : kOne);
     T P0[2][2], P1[2][2]; // [qw][qv]: along u with (a0, a1), and with l_1 (U jobs)
 #pragma unroll
     for (int qw = 0; qw < 2; ++qw)
@@ -949,15 +993,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       for (int qv = 0; qv < 2; ++qv)
       {
         P0[qw][qv] = dot2(a0, F[qw][qv][0], a1, F[qw][qv][1]);
-        P1[qw][qv] = dot2(cst<T>(B), F[qw][qv][0], cst<T>(A), F[qw][qv][1]);
+        P1[qw][qv] = dot2(kB, F[qw][qv][0], kA, F[qw][qv][1]);
       }
     // row r along v: classes W_r (sum jobs, r < 3) or l_(r & 1) of P0 / P1 (U jobs)
-    constexpr double kS0[4] = {AA, BB, AB, 0.}, kS1[4] = {BB, AA, AB, 0.};
+    constexpr T kS0[4] = {kAA, kBB, kAB, kZero}, kS1[4] = {kBB, kAA, kAB, kZero};
+    T * const tj = tab + l * 12 * kRow + slot;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
     {
-      T const x0 = isU ? cst<T>((r & 1) ? B : A) : cst<T>(kS0[r]);
-      T const x1 = isU ? cst<T>((r & 1) ? A : B) : cst<T>(kS1[r]);
+      T const x0 = isU ? ((r & 1) ? kB : kA) : kS0[r];
+      T const x1 = isU ? ((r & 1) ? kA : kB) : kS1[r];
       T R[2];
 #pragma unroll
       for (int qw = 0; qw < 2; ++qw)
@@ -967,77 +1012,88 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
         R[qw] = dot2(x0, s0, x1, s1);
       }
       // classes along w
-      sh.u.tab[l * 12 + r * 3 + 0] = dot2(cst<T>(AA), R[0], cst<T>(BB), R[1]);
-      sh.u.tab[l * 12 + r * 3 + 1] = dot2(cst<T>(BB), R[0], cst<T>(AA), R[1]);
-      sh.u.tab[l * 12 + r * 3 + 2] = cst<T>(AB) * (R[0] + R[1]);
+      tj[(r * 3 + 0) * kRow] = dot2(kAA, R[0], kBB, R[1]);
+      tj[(r * 3 + 1) * kRow] = dot2(kBB, R[0], kAA, R[1]);
+      tj[(r * 3 + 2) * kRow] = kAB * (R[0] + R[1]);
     }
   }
   __syncthreads();
 
-  // ---- C. entries, lane l = pairs l, l + 8, ...
+  // ---- C. entries: lane = slot s; a warp takes the pairs p = p0, p0 + 8, ... of 32 slots
+  int const warp = threadIdx.x >> 5;
+  int const s = 32 * (warp % SW) + (threadIdx.x & 31);
+  int64_t const gs = (int64_t)blockIdx.x * NS + s;
+  bool const liveS = gs < a.nelem;
   bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
   bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
-  double const kfac = a.kE ? a.kE[e] : 1.0;
-  // operator coefficients, applied in FP64 to the converted entry values (the FP64
-  // pipe has room; a double-float product and a conversion per operator cost more)
-  double ks[2], ms[2];
+  bool const needKE = (a.op[0].on && a.op[0].stiff == 2) || (a.op[1].on && a.op[1].stiff == 2);
+  double const kfac = (needKE && a.kE) ? a.kE[elemOf(a, liveS ? gs : a.nelem - 1)] : 1.0;
+  // operator coefficients in the arithmetic of the tables: the only FP64 instruction
+  // of an entry is then the addition in its conversion to double (the FP64 pipe, at
+  // 1/64 of the FP32 rate, is the scarcer resource)
+  T ks[2], ms[2];
 #pragma unroll
   for (int m = 0; m < 2; ++m)
   {
     LhsDev const & op = a.op[m];
-    ks[m] = op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.;
-    ms[m] = op.mass ? op.mc : 0.;
+    ks[m] = fromDouble<T>(op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.);
+    ms[m] = fromDouble<T>(op.mass ? op.mc : 0.);
   }
-  T const * tb = sh.u.tab;
-  for (int k = 0; k < 5; ++k)
+  uint32_t const * const ss = slotw + s * kSlotWords;
+  double const * const bs = bvAll + s * kBvStride;
+  uint32_t const consS = ss[kSwCons];
+  bool const anyBcS = consS && ((a.op[0].on && a.op[0].bc) || (a.op[1].on && a.op[1].bc));
+  char const * const col = reinterpret_cast<char const *>(tab + s);
+  char const * const rk = reinterpret_cast<char const *>(ss + kSwRank);
+  uint4 const * const pt = reinterpret_cast<uint4 const *>(NS == 32 ? kPairs32.w : kPairs64.w);
+  for (int p = warp / SW; p < 36; p += 8)
   {
-    int const p = l + 8 * k;
-    if (p >= 36)
-      break;
-    uint4 const d = sDesc[p];
-    int const i = d.x & 7, j = (d.x >> 3) & 7, cx = (d.x >> 6) & 3;
-    uint32_t const neg = d.x >> 8;
+    uint4 const d0 = __ldg(pt + 6 * p), d1 = __ldg(pt + 6 * p + 1), d2 = __ldg(pt + 6 * p + 2);
+    uint4 const d3 = __ldg(pt + 6 * p + 3), d4 = __ldg(pt + 6 * p + 4), d5 = __ldg(pt + 6 * p + 5);
     T kv = cst<T>(0.0), mv = cst<T>(0.0);
     if (needK)
     {
-      auto acc = sumStart(negIf(tb[d.y & 0xffu], neg & 1u));
-      sumAdd(acc, negIf(tb[(d.y >> 8) & 0xffu], (neg >> 1) & 1u));
-      sumAdd(acc, negIf(tb[(d.y >> 16) & 0xffu], (neg >> 2) & 1u));
-      sumAdd(acc, negIf(tb[d.y >> 24], (neg >> 3) & 1u));
-      sumAdd(acc, negIf(tb[d.z & 0xffu], (neg >> 4) & 1u));
-      sumAdd(acc, negIf(tb[(d.z >> 8) & 0xffu], (neg >> 5) & 1u));
-      sumAdd(acc, negIf(tb[(d.z >> 16) & 0xffu], (neg >> 6) & 1u));
-      sumAdd(acc, negIf(tb[d.z >> 24], (neg >> 7) & 1u));
-      sumAdd(acc, negIf(tb[d.w & 0xffu], (neg >> 8) & 1u));
+      auto acc = sumStartS(ldTab<T>(col, d0.x), d2.y);
+      sumAddS(acc, ldTab<T>(col, d0.y), d2.z);
+      sumAddS(acc, ldTab<T>(col, d0.z), d2.w);
+      sumAddS(acc, ldTab<T>(col, d0.w), d3.x);
+      sumAddS(acc, ldTab<T>(col, d1.x), d3.y);
+      sumAddS(acc, ldTab<T>(col, d1.y), d3.z);
+      sumAddS(acc, ldTab<T>(col, d1.z), d3.w);
+      sumAddS(acc, ldTab<T>(col, d1.w), d4.x);
+      sumAddS(acc, ldTab<T>(col, d2.x), d4.y);
       kv = sumEnd(acc);
     }
     if (needM)
     {
-      uint32_t const mo = d.w >> 8;
-      T const alpha = cx == 2 ? cst<T>(AB) : cst<T>(kAlpha01);
-      T const beta = negIf(cx == 2 ? cst<T>(0.0) : cst<T>(kBeta0), cx == 1);
-      mv = dot2(alpha, tb[mo], beta, tb[mo + 12]);
+      constexpr T kAB = cst<T>(AB), kA01 = cst<T>(kAlpha01), kB0 = cst<T>(kBeta0), kZero = cst<T>(0.0);
+      uint32_t const cx = d5.x;
+      T const alpha = cx == 2 ? kAB : kA01;
+      T const beta = negIf(cx == 2 ? kZero : kB0, cx == 1);
+      mv = dot2(alpha, ldTab<T>(col, d4.z), beta, ldTab<T>(col, d4.w));
     }
-    double const kd = needK ? toDouble(kv) : 0., md = needM ? toDouble(mv) : 0.;
-    bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
+    int const i = d5.y & 7, j = d5.y >> 3;
+    uint32_t const pij = ss[kSwRp + i] + *reinterpret_cast<uint16_t const *>(rk + (d5.z & 0xffffu));
+    uint32_t const pji = ss[kSwRp + j] + *reinterpret_cast<uint16_t const *>(rk + (d5.z >> 16));
+    bool const ci = (consS >> i) & 1u, cj = (consS >> j) & 1u;
 #pragma unroll
     for (int m = 0; m < 2; ++m)
     {
       LhsDev const & op = a.op[m];
       if (!op.on)
         continue;
-      double const val = op.stiff ? (op.mass ? fma(ks[m], kd, ms[m] * md) : ks[m] * kd) : ms[m] * md;
-      if (!live)
+      double const val = toDouble(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
+      if (!liveS)
         continue;
-      if (anyBc && op.bc && (ci || cj))
+      if (anyBcS && op.bc && (ci || cj))
       {
-        condenseEntry(op.vals + sh.rp[i] + sh.rank[i * 9], a.bcDiag, a.b, sh.dof[i], sh.dof[j], sh.bv[i], sh.bv[j],
-                      ci, cj, i == j, val);
+        condenseEntry(op.vals + pij, a.bcDiag, a.b, ss[kSwDof + i], ss[kSwDof + j], bs[i], bs[j], ci, cj, i == j,
+                      val);
         continue;
       }
-      atomicAdd(op.vals + sh.rp[i] + sh.rank[i * 8 + j], val);
+      atomicAdd(op.vals + pij, val);
       if (i != j)
-        atomicAdd(op.vals + sh.rp[j] + sh.rank[j * 8 + i], val);
+        atomicAdd(op.vals + pji, val);
     }
   }
 }
@@ -1063,8 +1119,6 @@ void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThre
   int const nt = threads ? threads : q1g::kThreads;
   if (fp64)
     go(q1g::kAssembleQ1Group<double, q1g::kThreads>, q1g::kThreads, q1g::smemBytes<q1g::kThreads>());
-  else if (nt == 128)
-    go(q1g::kAssembleQ1Group<dfl, 128>, 128, q1g::smemBytes<128>());
   else if (nt == 512)
     go(q1g::kAssembleQ1Group<dfl, 512>, 512, q1g::smemBytes<512>());
   else
