@@ -117,3 +117,53 @@ def compare_csr(g, o, ndof, tol=TOL):
         assert abs(v) <= ROUNDOFF_BAND * rowmax[r], f"pattern differs at ({r},{c}) with |v|={abs(v):.3e}"
         n_band += 1
     return n_band
+
+
+# ---------------------------------------------------------------- full-size properties
+def nnz_q1_cube(n):
+    """Structural nnz of Q1 hexahedra on an n^3 cube: the 1D count 3n + 1, cubed."""
+    return (3 * n + 1) ** 3
+
+
+def nnz_p2_kuhn6(n):
+    """Structural nnz of P2 tetrahedra on an n^3 cube split into 6 Kuhn tetrahedra per
+    cell (a cubic in n, fitted to brute-force counts and checked against them)."""
+    return 230 * n ** 3 + 138 * n ** 2 + 24 * n + 1
+
+
+# Q1 reference element: node n sits at lattice position (x, y, z) with the vertex order
+# of the hexahedron (bottom face counter-clockwise, then the top face)
+_HEX_NODES = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+
+
+def q1_quadrature(xyz, conn, k=None, chunk=131072):
+    """Per-mesh sums by the 2x2x2 Gauss rule on the trilinear map, in numpy:
+    (sum_e vol_e, sum_e k_e vol_e, sum_e sum_q |det J_q| f(x_q)) with
+    f = sin(pi x) sin(pi y) sin(pi z) at the reference's quadrature point
+    x_q = (vertex average) + J_q xi_q (curfe.hpp:92-94, geo.hpp:721-728)."""
+    g = 1.0 / np.sqrt(3.0)
+    s = 2 * _HEX_NODES - 1                          # node signs, (8, 3)
+    xi = s * g                                      # Gauss points in the node order, (8, 3)
+    # dN_n/dxi_c at xi_q: s_nc / 8 * prod_{d != c} (1 + s_nd xi_qd)
+    f1 = 1.0 + xi[:, None, :] * s[None, :, :]       # (q, n, d)
+    dN = np.empty((8, 8, 3))
+    for c in range(3):
+        others = [d for d in range(3) if d != c]
+        dN[:, :, c] = s[None, :, c] / 8.0 * f1[:, :, others[0]] * f1[:, :, others[1]]
+    dN2 = dN.transpose(1, 0, 2).reshape(8, 24)     # (n, q * 3 + c)
+    vol = kvol = rhs = 0.0
+    for e0 in range(0, conn.shape[0], chunk):
+        X = xyz[conn[e0:e0 + chunk].astype(np.int64)]           # (e, n, 3)
+        J = (X.transpose(0, 2, 1) @ dN2).reshape(-1, 3, 8, 3)  # J[e, r, q, c]
+        det = np.abs(J[:, 0, :, 0] * (J[:, 1, :, 1] * J[:, 2, :, 2] - J[:, 1, :, 2] * J[:, 2, :, 1])
+                     - J[:, 0, :, 1] * (J[:, 1, :, 0] * J[:, 2, :, 2] - J[:, 1, :, 2] * J[:, 2, :, 0])
+                     + J[:, 0, :, 2] * (J[:, 1, :, 0] * J[:, 2, :, 1] - J[:, 1, :, 1] * J[:, 2, :, 0]))  # (e, q)
+        org = X.mean(axis=1)                                    # (e, 3)
+        xq = org[:, :, None] + np.einsum("erqc,qc->erq", J, xi)  # (e, r, q)
+        fq = np.prod(np.sin(np.pi * xq), axis=1)                # (e, q)
+        ve = det.sum(axis=1)
+        vol += ve.sum()
+        if k is not None:
+            kvol += (k[e0:e0 + chunk] * ve).sum()
+        rhs += (det * fq).sum()
+    return vol, kvol, rhs

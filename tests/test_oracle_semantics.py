@@ -86,3 +86,37 @@ def test_openmp_equals_serial(oracle_lib):
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
     assert np.array_equal(ba, bb)
+
+
+@pytest.mark.parametrize("t,gen,closed", [(O.Q1HEX, "hex", "nnz_q1_cube"), (O.P2TET, "tet6", "nnz_p2_kuhn6")])
+def test_structural_nnz_closed_forms(t, gen, closed):
+    """The closed forms the full-size GPU tests use, against brute-force counts of the
+    DOF pairs that share an element."""
+    import helpers as H
+
+    for n in range(1, 7):
+        xyz, conn = H.GEN[gen](n)
+        em, ndof = O.dofmap(t, xyz.shape[0], conn)
+        N = em.shape[1]
+        i = np.repeat(em, N, axis=1).reshape(-1).astype(np.int64)
+        j = np.tile(em, (1, N)).reshape(-1).astype(np.int64)
+        assert np.unique(i * ndof + j).size == getattr(H, closed)(n), n
+
+
+def test_q1_quadrature_helper_matches_oracle():
+    """The numpy quadrature of the full-size checks reproduces the oracle's element loop."""
+    import helpers as H
+
+    xyz, conn, k = H.problem("hex", 5, 0.2, seed=3, sigma=1.0)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    vol, kvol, rsum = H.q1_quadrature(xyz, conn, k)
+    K, b = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs={"stiff_kind": 2, "k_e": k},
+                   rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0})
+    Ks = O.csr_to_scipy(K, ndof)
+    X = np.empty((ndof, 3))
+    X[em.reshape(-1)] = xyz[conn.reshape(-1).astype(np.int64)]
+    assert abs(vol - 1.0) <= 1e-13
+    for d in range(3):
+        u = X[:, d] - 0.5
+        assert abs(u @ (Ks @ u) - kvol) <= 1e-12 * kvol
+    assert abs(b.sum() - rsum) <= 1e-13 * rsum
