@@ -185,6 +185,64 @@ def measure_widened(xyz, conn, n_stokes=16):
     return out
 
 
+def measure_configs(peak_gbs, reps=5):
+    """The other element types on their own workloads: the P1 16^3 x 6 Poisson case
+    (K + unit load, k = 1), the P2 64^3 x 6 case (perturbed 0.15 h, k_e lognormal(0, 0.5),
+    K + M) and Q2 48^3 hexahedra (perturbed 0.2 h, K + M + sin3 load).  Best of `reps`
+    event-timed assemblies each, with the algorithmic bytes of one assembly (vertex ids,
+    DOF map, k_e, coordinates, value and load writes) against the HBM peak."""
+    import torch
+
+    from proxpde_gb300 import _lib as L
+    from proxpde_gb300 import Context, meshgen
+
+    out = {}
+    cases = (("p1tet_16", L.P1TET, meshgen.cube_tet6, 16, 0.0, None, 1, {"kind": 1, "fn": L.FN_CONST, "coef": 1.0},
+              "kAssembleTet<P1>"),
+             ("p2tet_64", L.P2TET, meshgen.cube_tet6, 64, 0.15, 0.5, 2, None, "kAssembleTet<P2>"),
+             ("q2hex_48", L.Q2HEX, meshgen.cube_hex, 48, 0.2, 1.0, 2, {"kind": 1, "fn": L.FN_SIN3, "coef": 1.0},
+              "kAssemble<Q2>"))
+    for name, t, gen, n, alpha, sigma, nmat, rhs, kern in cases:
+        xyz, conn = gen(n)
+        if alpha:
+            xyz = meshgen.perturb(xyz, n, alpha, 20261211)
+        E = conn.shape[0]
+        ctx = Context(0)
+        ctx.set_mesh(t, xyz, conn)
+        ndof = ctx.build_dofmap()
+        nnz = ctx.build_pattern()
+        opK = {"stiffness": 1, "stiff_coef": 1.0}
+        if sigma:
+            ctx.set_coef(meshgen.lognormal(20261212, E, sigma))
+            opK = {"stiffness": 2, "stiff_coef": 1.0}
+        K = torch.empty(nnz, dtype=torch.float64, device="cuda")
+        M = torch.empty_like(K) if nmat == 2 else None
+        b = torch.empty(ndof, dtype=torch.float64, device="cuda") if rhs else None
+        kw = dict(op0=opK, vals0=K, op1={"mass": 1, "mass_coef": 1.0} if M is not None else None, vals1=M, rhs=rhs, b=b)
+        for _ in range(2):
+            ctx.assemble(**kw)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            ctx.assemble(**kw)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = min(ts)
+        N = {L.P1TET: 4, L.P2TET: 10, L.Q1HEX: 8, L.Q2HEX: 27}[t]
+        B = 4 * conn.shape[1] * E + 4 * N * E + (8 * E if sigma else 0) + 24 * xyz.shape[0] + 8 * nnz * nmat + \
+            (8 * ndof if rhs else 0)
+        gbs = B / (ms * 1e-3) / 1e9
+        out[name] = {"elements": int(E), "ndof": int(ndof), "nnz": int(nnz), "ms": ms, "elements_per_s": E / (ms * 1e-3),
+                     "kernel": kern, "algorithmic_bytes": int(B), "achieved_gbs": gbs, "frac_hbm": gbs / peak_gbs,
+                     "includes": "memset of the outputs + element kernel"}
+        del ctx, K, M, b
+        torch.cuda.empty_cache()
+    return out
+
+
 def measure_adjoint(n=96, reps=2):
     """Adjoint gradient dJ/dlog k_e on the perturbed Q1 96^3 cube (Dirichlet on all faces,
     f = 1, u_t = sin sin sin), device Jacobi-CG to 1e-10: forward + backward time."""
@@ -331,6 +389,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default kernels)")
     ap.add_argument("--no-widened", action="store_true", help="skip the Dirichlet-setup and Stokes measurements")
+    ap.add_argument("--no-configs", action="store_true", help="skip the P1 / P2 / Q2 workload measurements")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-gradient measurement")
@@ -491,9 +550,11 @@ def main():
                "sample": f"{args.cpu_n}^3 Q1 hexes of the same workload (K+M+rhs), oracle restatement with OpenMP",
                "value_1thread": v_one, "sample_1thread": f"{min(args.cpu_n, 24)}^3 hexes, 1 thread"}
 
-    adjoint = batched = widened = None
+    adjoint = batched = widened = configs = None
     if rank == 0 and not args.no_widened:
         widened = measure_widened(xyz, conn)
+    if rank == 0 and not args.no_configs:
+        configs = measure_configs(hbm)
     if rank == 0 and not args.no_adjoint:
         adjoint = measure_adjoint()
     if rank == 0 and not args.no_batched:
@@ -508,7 +569,7 @@ def main():
                        "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned), "tuning": tuning,
                        "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
                        "setup_s": setup_s, "parallelism": f"replicas x{world}"},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "widened": widened,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "widened": widened, "configs": configs,
             "gpu_launches": 3 * args.steps, "adjoint": adjoint, "batched": batched,
         }
         print(json.dumps(line), flush=True)

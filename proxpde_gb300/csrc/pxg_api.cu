@@ -123,6 +123,8 @@ pxg_status pxg_create(pxg_ctx ** out, int device)
   c->q1Generic = gen && gen[0] == '1';
   char const * f64 = getenv("PXG_Q1_FP64");
   c->q1Fp64 = f64 && f64[0] == '1';
+  char const * tf64 = getenv("PXG_TET_FP64");
+  c->tetFp64 = tf64 && tf64[0] == '1';
   char const * thr = getenv("PXG_Q1_THREAD");
   c->q1Thread = thr && thr[0] == '1';
   pxg_status s = ensureDevice(c);

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <vector>
 
+#include "pxg_dfl.h"
 #include "pxg_internal.h"
 
 namespace pxg
@@ -33,6 +34,9 @@ __constant__ double cP2phi[11 * 10], cP2dphi[11 * 10 * 3], cP2w[11], cP2xi[11 * 
     cP2M[100];
 __constant__ double cQ1phi[8 * 8], cQ1dphi[8 * 8 * 3], cQ1w[8], cQ1xi[8 * 3];
 __constant__ double cQ2phi[27 * 27], cQ2dphi[27 * 27 * 3], cQ2w[27], cQ2xi[27 * 3];
+// the affine elements' reference tensors as hi/lo float pairs (kAssembleTet)
+__constant__ float2 cP1Td[6 * 16], cP1Md[16], cP2Td[6 * 100], cP2Md[100];
+__constant__ double cP1I[4], cP2I[10]; // sum_q w_q phi_i(q): the load vector of f = 1
 
 template <int T>
 __device__ __forceinline__ double PHI(int q, int i)
@@ -261,6 +265,29 @@ pxg_status initTables(pxg_ctx * c)
             }
             M[i * N + j] += w[q] * phi[q * N + i] * phi[q * N + j];
           }
+      // the same as hi/lo float pairs, and sum_q w_q phi_i(q), for kAssembleTet
+      std::vector<float2> Td(T.size()), Md(M.size());
+      auto split = [](double x) { float const h = (float)x; return make_float2(h, (float)(x - (double)h)); };
+      for (size_t k = 0; k < T.size(); ++k)
+        Td[k] = split(T[k]);
+      for (size_t k = 0; k < M.size(); ++k)
+        Md[k] = split(M[k]);
+      std::vector<double> I(N, 0.);
+      for (int q = 0; q < nq; ++q)
+        for (int i = 0; i < N; ++i)
+          I[i] += w[q] * phi[q * N + i];
+      if (t == P1TET)
+      {
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1Td, Td.data(), Td.size() * sizeof(float2)));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1Md, Md.data(), Md.size() * sizeof(float2)));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1I, I.data(), I.size() * 8));
+      }
+      else
+      {
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2Td, Td.data(), Td.size() * sizeof(float2)));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2Md, Md.data(), Md.size() * sizeof(float2)));
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP2I, I.data(), I.size() * 8));
+      }
       if (t == P1TET)
       {
         std::vector<double> d1(4 * 3);
@@ -584,6 +611,315 @@ __global__ void __launch_bounds__(NT) kAssemble(AsmArgs a)
   }
 }
 
+// ------------------------------------------- tetrahedra in double-float arithmetic
+// kAssembleTet: the P1/P2 element loop of kAssemble with the geometry and the entries
+// on the FP32 pipes (double-float, pxg_dfl.h).  At 1/64 of the FP32 rate, the FP64
+// pipe bounds the FP64 form of this loop (ncu, P2 32^3: FP64 pipe 82 % busy, issue
+// 12 %).  Per element: J from the vertex differences (FP64 subtractions, exact
+// conversions), adj(J), |det J| and G = adj adj^T / |det J| in double-float; an entry
+// is the six-term product of G with the reference tensor (its hi/lo float pairs in
+// constant memory, errors gathered in one float), the mass entry |det J| Mhat_ij.  A
+// single stiffness (mass) operator's coefficient is folded into G (|det J|) once per
+// element.  The values are converted to double with one FP64 addition each; BC
+// condensation and the load vector follow kAssemble in FP64.
+
+template <int T>
+__device__ __forceinline__ dfl TTd(int c, int i, int j)
+{
+  float2 const v = T == P1TET ? cP1Td[(c * 4 + i) * 4 + j] : cP2Td[(c * 10 + i) * 10 + j];
+  return dfl{v.x, v.y};
+}
+template <int T>
+__device__ __forceinline__ dfl MHATd(int i, int j)
+{
+  float2 const v = T == P1TET ? cP1Md[i * 4 + j] : cP2Md[i * 10 + j];
+  return dfl{v.x, v.y};
+}
+template <int T>
+__device__ __forceinline__ double PINT(int i)
+{
+  return T == P1TET ? cP1I[i] : cP2I[i];
+}
+
+// sum_k g_k t_k over six double-float pairs: exact high products (FMA TwoProd), their
+// sum by TwoSum, every term of order 2^-24 gathered in one float, one renormalisation
+__device__ __forceinline__ dfl dot6(dfl const (&g)[6], dfl const (&t)[6])
+{
+  float p[6], lo = 0.f;
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+  {
+    p[k] = __fmul_rn(g[k].h, t[k].h);
+    float e = __fmaf_rn(g[k].h, t[k].h, -p[k]);
+    e = __fmaf_rn(g[k].h, t[k].l, e);
+    e = __fmaf_rn(g[k].l, t[k].h, e);
+    lo = __fadd_rn(lo, e);
+  }
+  float s = p[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k)
+  {
+    dfl const r = dflTwoSum(s, p[k]);
+    s = r.h;
+    lo = __fadd_rn(lo, r.l);
+  }
+  return dflFastTwoSum(s, lo);
+}
+
+// v[i] for a run-time i by a chain of selects: v stays in registers
+template <typename V, int N>
+__device__ __forceinline__ V pickN(V const (&v)[N], int i)
+{
+  V r = v[0];
+#pragma unroll
+  for (int n = 1; n < N; ++n)
+    r = i == n ? v[n] : r;
+  return r;
+}
+
+// Dirichlet condensation of one entry (builder.hpp:76-124): a constrained diagonal
+// takes bcDiag, a free row the lift -K_ij h_j, added to b at once.  Out of line: its
+// FP64 code would otherwise be predicated into every entry.
+__device__ __noinline__ void condenseTet(double * diag, double bcDiag, double * b, uint32_t dofi, uint32_t dofj,
+                                         double const * bcVal, bool ci, bool cj, bool isDiag, double val)
+{
+  if (isDiag)
+  {
+    atomicAdd(diag, bcDiag);
+    return;
+  }
+  if (!b)
+    return;
+  if (!ci)
+  {
+    double const t = val * bcVal[dofj];
+    if (t != 0.)
+      atomicAdd(b + dofi, -t);
+  }
+  if (!cj)
+  {
+    double const t = val * bcVal[dofi];
+    if (t != 0.)
+      atomicAdd(b + dofj, -t);
+  }
+}
+
+template <int T, int NT>
+__global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
+{
+  constexpr int N = Elem<T>::N, NQ = Elem<T>::NQ;
+  int64_t const i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i0 >= a.nelem)
+    return;
+  int64_t const e = elemOf(a, i0);
+
+  double X[4][3];
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+  {
+    uint32_t const id = a.conn[e * 4 + v];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      X[v][d] = a.xyz[3 * (int64_t)id + d];
+  }
+  uint32_t dof[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    dof[i] = a.emap[e * N + i];
+  uint32_t cons = 0;
+  if (a.bcMask)
+  {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (a.bcMask[dof[i]])
+        cons |= 1u << i;
+  }
+  LhsDev const & op0 = a.op[0];
+  LhsDev const & op1 = a.op[1];
+  bool const k0 = op0.on && op0.stiff, k1 = op1.on && op1.stiff;
+  bool const m0 = op0.on && op0.mass, m1 = op1.on && op1.mass;
+  bool const needK = k0 || k1, needM = m0 || m1;
+  bool const kE = (k0 && op0.stiff == 2) || (k1 && op1.stiff == 2);
+  double const kfac = (kE && a.kE) ? a.kE[e] : 1.0;
+
+  // --- geometry in double-float: J columns = vertex differences
+  dfl J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc)
+      J[r][cc] = toDfl(X[cc + 1][r] - X[0][r]);
+  dfl A[3][3];
+  A[0][0] = dot2(J[1][1], J[2][2], -J[1][2], J[2][1]);
+  A[0][1] = dot2(J[0][2], J[2][1], -J[0][1], J[2][2]);
+  A[0][2] = dot2(J[0][1], J[1][2], -J[0][2], J[1][1]);
+  A[1][0] = dot2(J[1][2], J[2][0], -J[1][0], J[2][2]);
+  A[1][1] = dot2(J[0][0], J[2][2], -J[0][2], J[2][0]);
+  A[1][2] = dot2(J[0][2], J[1][0], -J[0][0], J[1][2]);
+  A[2][0] = dot2(J[1][0], J[2][1], -J[1][1], J[2][0]);
+  A[2][1] = dot2(J[0][1], J[2][0], -J[0][0], J[2][1]);
+  A[2][2] = dot2(J[0][0], J[1][1], -J[0][1], J[1][0]);
+  dfl const det = dot3(J[0][0], A[0][0], J[0][1], A[1][0], J[0][2], A[2][0]);
+  dfl const adet = fabs(det);
+  // operator coefficients: a single stiffness (mass) operator's is folded into G (|det J|)
+  bool const foldK = k0 != k1, foldM = m0 != m1;
+  double const ks0 = k0 ? (op0.stiff == 2 ? op0.sc * kfac : op0.sc) : 0.;
+  double const ks1 = k1 ? (op1.stiff == 2 ? op1.sc * kfac : op1.sc) : 0.;
+  double const ms0 = m0 ? op0.mc : 0., ms1 = m1 ? op1.mc : 0.;
+  dfl G[6];
+  {
+    dfl const s = fromDouble<dfl>(foldK ? (k0 ? ks0 : ks1) : 1.0) * rcp(adet);
+    G[0] = s * dot3(A[0][0], A[0][0], A[0][1], A[0][1], A[0][2], A[0][2]);
+    G[1] = s * dot3(A[1][0], A[1][0], A[1][1], A[1][1], A[1][2], A[1][2]);
+    G[2] = s * dot3(A[2][0], A[2][0], A[2][1], A[2][1], A[2][2], A[2][2]);
+    G[3] = s * dot3(A[0][0], A[1][0], A[0][1], A[1][1], A[0][2], A[1][2]);
+    G[4] = s * dot3(A[0][0], A[2][0], A[0][1], A[2][1], A[0][2], A[2][2]);
+    G[5] = s * dot3(A[1][0], A[2][0], A[1][1], A[2][1], A[1][2], A[2][2]);
+  }
+  dfl const am = foldM ? fromDouble<dfl>(m0 ? ms0 : ms1) * adet : adet;
+  dfl const kd0 = fromDouble<dfl>(ks0), kd1 = fromDouble<dfl>(ks1);
+  dfl const md0 = fromDouble<dfl>(ms0), md1 = fromDouble<dfl>(ms1);
+
+  // --- entries.  Row i is a run-time loop for P2 (a compile-time one for P1); the
+  // columns j are unrolled, so that the element's DOFs and row pointers stay in
+  // registers (a run-time index would move them to local memory, and every entry
+  // would wait on a local load, then on the dependent rowPtr load).
+  int32_t rpn[N];
+#pragma unroll
+  for (int n = 0; n < N; ++n)
+    rpn[n] = a.rowPtr[dof[n]];
+  bool const anyBc = cons && ((op0.on && op0.bc) || (op1.on && op1.bc));
+  uint16_t const * rk = a.rank + e * (int64_t)(N * N);
+  constexpr int kRowUnroll = N <= 4 ? N : 1; // P1: the 10 entries fully unrolled
+#pragma unroll kRowUnroll
+  for (int i = 0; i < N; ++i)
+  {
+    uint32_t const dofi = pickN(dof, i);
+    int32_t const rpi = pickN(rpn, i);
+    bool const ci = (cons >> i) & 1u;
+#pragma unroll
+    for (int j = 0; j < N; ++j)
+    {
+      if (j < i)
+        continue; // uniform: every thread is in row i
+      dfl kv = dfl{0.f, 0.f}, mv = dfl{0.f, 0.f};
+      if (needK)
+      {
+        dfl t[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+          t[k] = TTd<T>(k, i, j);
+        kv = dot6(G, t);
+      }
+      if (needM)
+        mv = am * MHATd<T>(i, j);
+      int32_t const pij = rpi + rk[i * N + j];
+      int32_t const pji = rpn[j] + rk[j * N + i];
+      bool const cj = (cons >> j) & 1u;
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+      {
+        LhsDev const & op = a.op[m];
+        if (!op.on)
+          continue;
+        dfl v;
+        if (op.stiff)
+        {
+          v = foldK ? kv : (m ? kd1 : kd0) * kv;
+          if (op.mass)
+            v = v + (foldM ? mv : (m ? md1 : md0) * mv);
+        }
+        else
+          v = foldM ? mv : (m ? md1 : md0) * mv;
+        double const val = toDouble(v);
+        if (anyBc && op.bc && (ci || cj))
+        {
+          condenseTet(op.vals + pij, a.bcDiag, a.b, dofi, dof[j], a.bcVal, ci, cj, i == j, val);
+          continue;
+        }
+        red(op.vals + pij, val);
+        if (j != i)
+          red(op.vals + pji, val);
+      }
+    }
+  }
+  if (!a.b)
+    return;
+  // Dirichlet values at the constrained DOFs, once per operator with BCs (buildLhs)
+  if (anyBc)
+  {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+    {
+      if (!a.op[m].on || !a.op[m].bc)
+        continue;
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+        if ((cons >> n) & 1u)
+        {
+          double const h = a.bcVal[dof[n]];
+          if (h != 0.)
+            red(a.b + dof[n], h);
+        }
+    }
+  }
+  if (!a.rkind)
+    return;
+  // load vector (buildRhs: b += C Fe), in FP64
+  double const adetD = toDouble(adet);
+  if (a.rkind == 1 && a.fn == PXG_FN_CONST)
+  {
+    // f = c: Fe_i = c |det J| sum_q w_q phi_i(q)
+    double const f = evalFn(a.fn, a.rc, 0., 0., 0.) * adetD;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (!(a.rbc && ((cons >> i) & 1u)))
+        red(a.b + dof[i], f * PINT<T>(i));
+    return;
+  }
+  double fq[NQ];
+  if (a.rkind == 1)
+  {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double xq[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        xq[r] = X[0][r] + ((X[1][r] - X[0][r]) * XI<T>(q, 0) + (X[2][r] - X[0][r]) * XI<T>(q, 1) +
+                           (X[3][r] - X[0][r]) * XI<T>(q, 2));
+      fq[q] = evalFn(a.fn, a.rc, xq[0], xq[1], xq[2]);
+    }
+  }
+  else
+  {
+    double loc[N];
+#pragma unroll
+    for (int n = 0; n < N; ++n)
+      loc[n] = a.field[dof[n]];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double s = 0.;
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+        s += PHI<T>(q, n) * loc[n];
+      fq[q] = a.rc * s;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+  {
+    if (a.rbc && ((cons >> i) & 1u))
+      continue;
+    double fe = 0.;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      fe += (adetD * WQ<T>(q)) * PHI<T>(q, i) * fq[q];
+    red(a.b + dof[i], fe);
+  }
+}
+
 template <int T>
 __global__ void kInterpolate(int64_t nelem, double const * __restrict__ xyz, uint32_t const * __restrict__ conn,
                              uint32_t const * __restrict__ emap, int fn, double c, double * __restrict__ v)
@@ -777,6 +1113,20 @@ namespace
 // Threads per block: 64, 128 or 256 for the tetrahedra (autotuner candidates), 128
 // for the hexahedra of the generic kernel.
 template <int T>
+void launchAssembleTet(AsmArgs const & a, cudaStream_t s, int threads)
+{
+  auto go = [&](auto kern, int nt) {
+    unsigned const blocks = (unsigned)((a.nelem + nt - 1) / nt);
+    kern<<<blocks, nt, 0, s>>>(a);
+  };
+  if (threads == 64)
+    return go(kAssembleTet<T, 64>, 64);
+  if (threads == 256)
+    return go(kAssembleTet<T, 256>, 256);
+  go(kAssembleTet<T, 128>, 128);
+}
+
+template <int T>
 void launchAssemble(AsmArgs const & a, cudaStream_t s, int threads)
 {
   auto go = [&](auto kern, int nt) {
@@ -880,10 +1230,16 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     switch (c->etype)
     {
     case P1TET:
-      launchAssemble<P1TET>(la, s, c->threads);
+      if (c->tetFp64)
+        launchAssemble<P1TET>(la, s, c->threads);
+      else
+        launchAssembleTet<P1TET>(la, s, c->threads);
       break;
     case P2TET:
-      launchAssemble<P2TET>(la, s, c->threads);
+      if (c->tetFp64)
+        launchAssemble<P2TET>(la, s, c->threads);
+      else
+        launchAssembleTet<P2TET>(la, s, c->threads);
       break;
     case Q1HEX:
       if (c->q1Generic)

@@ -174,7 +174,7 @@ __host__ __device__ constexpr dfl cst<dfl>(double x)
 
 // Rare path of toDfl (magnitudes outside 2^-74 .. 2^127): kept out of line, so that
 // the compiler does not predicate its FP64-pipe conversions into every call.
-__device__ __noinline__ dfl toDflSlow(double x)
+static __device__ __noinline__ dfl toDflSlow(double x)
 {
   float const h = __double2float_rn(x);
   return dfl{h, __double2float_rn(x - (double)h)};

@@ -322,6 +322,7 @@ struct pxg_ctx
   // generic kernel (both kept for cross-checks)
   bool q1Generic = false;
   bool q1Fp64 = false;
+  bool tetFp64 = false; // P1/P2: the FP64 element kernel instead of kAssembleTet
   bool q1Thread = false;
   CgWork cg;
   AdjState adj;

@@ -189,3 +189,50 @@ def test_q1_kernels_agree_with_oracle(engine, monkeypatch, kernel, bc, n):
     compare_csr(g["mats"][0], csrK, ndof)
     compare_csr(g["mats"][1], csrM, ndof)
     assert_close(g["b"], b, what="rhs")
+
+
+@pytest.mark.parametrize("kernel", ["dfl", "fp64"])
+@pytest.mark.parametrize("t,gen,n", [(O.P1TET, "tet6", 9), (O.P2TET, "tet6", 5), (O.P2TET, "tet5", 4)],
+                         ids=["p1tet6", "p2tet6", "p2tet5"])
+@pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
+@pytest.mark.parametrize("rhs_fn", ["const", "sin3"])
+def test_tet_kernels_agree_with_oracle(engine, monkeypatch, kernel, t, gen, n, bc, rhs_fn):
+    """The tetrahedron kernels against the oracle: double-float entries (default) and
+    FP64 (PXG_TET_FP64=1); K(k_e) + M with a load (the constant load takes the
+    closed-form path of the double-float kernel), with and without inhomogeneous
+    Dirichlet data."""
+    monkeypatch.setenv("PXG_TET_FP64", "1" if kernel == "fp64" else "0")
+    xyz, conn, k = problem(gen, n, 0.15, seed=23, sigma=0.5)
+    em, ndof = O.dofmap(t, xyz.shape[0], conn)
+    fn = O.FN_CONST if rhs_fn == "const" else O.FN_SIN3
+    ops = [dict(K_OP), {"mass": 1, "mass_coef": 1.5}]
+    rhs = {"kind": 1, "fn": fn, "coef": 2.0}
+    bcarg, mask, val = None, None, None
+    if bc:
+        dx = O.dof_coords(t, xyz, conn, em, ndof)
+        mask = O.plane_bc_mask(dx, [("x", 0.0), ("y", 1.0)])
+        val = np.where(mask, 0.25 + dx[:, 2], 0.0)
+        dofs = np.nonzero(mask)[0].astype(np.uint32)
+        bcarg = (dofs, val[dofs])
+        ops[0]["apply_bc"] = 1
+        rhs["apply_bc"] = 1
+    g = gpu_assemble(t, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg)
+    csrK, b = O.build(t, xyz, conn, em, ndof, lhs=oracle_lhs(ops[0], k), bc_mask=mask, bc_val=val)
+    csrM, _ = O.build(t, xyz, conn, em, ndof, lhs=oracle_lhs(ops[1], k))
+    _, b = O.build(t, xyz, conn, em, ndof, rhs={"kind": 1, "fn": fn, "c": 2.0, "apply_bc": int(bc)},
+                   bc_mask=mask, bc_val=val, b=b)
+    compare_csr(g["mats"][0], csrK, ndof)
+    compare_csr(g["mats"][1], csrM, ndof)
+    assert_close(g["b"], b, what="rhs")
+
+
+def test_tet_two_stiffness_operators(engine):
+    """Two stiffness operators with different coefficients (no folding into G) and a
+    combined stiffness + mass operator, on P2."""
+    xyz, conn, k = problem("tet6", 4, 0.15, seed=29, sigma=0.5)
+    em, ndof = O.dofmap(O.P2TET, xyz.shape[0], conn)
+    ops = [{"stiffness": 2, "stiff_coef": 0.75, "mass": 1, "mass_coef": 2.0}, {"stiffness": 1, "stiff_coef": 3.0}]
+    g = gpu_assemble(O.P2TET, xyz, conn, ops, k=k)
+    for op, mat in zip(ops, g["mats"]):
+        csr, _ = O.build(O.P2TET, xyz, conn, em, ndof, lhs=oracle_lhs(op, k))
+        compare_csr(mat, csr, ndof)
