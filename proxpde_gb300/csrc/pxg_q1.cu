@@ -690,6 +690,10 @@ struct Smem
 {
   static constexpr int NS = NT / 8, kRow = NS + 1;
   static constexpr size_t tabBytes = (size_t)(96 * kRow > NS * kGStride ? 96 * kRow : NS * kGStride) * 8;
+  // phase D's scratch (centroid coordinates, their sin and cos) behind G in the table
+  // region, which the tables overwrite only in phase B
+  static constexpr size_t scratchOff = (size_t)NS * kGStride * 8;
+  static_assert(scratchOff + (size_t)NS * 3 * 24 <= tabBytes, "phase D scratch overlaps the next region");
   static constexpr size_t slotOff = (tabBytes + 15) / 16 * 16;
   static constexpr size_t bvOff = slotOff + ((size_t)NS * kSlotWords * 4 + 15) / 16 * 16;
   static constexpr size_t bytes = bvOff + (size_t)NS * kBvStride * 8;
@@ -926,14 +930,26 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
         }
         if (a.fn == PXG_FN_SIN3)
         {
-          int const dd = l < 3 ? l : 2;
-          double const od = pick3(X0, dd) + toDouble(scl(pick3(sY, dd), 0.125f));
-          T so, co;
-          sinCosPiG(od, so, co);
+          // sin and cos of pi times the centroid's coordinates: one thread per
+          // (element, coordinate) of the block, through shared memory behind G
+          double * const sOd = reinterpret_cast<double *>(smem + S::scratchOff); // [NS][3]
+          T * const sSo = reinterpret_cast<T *>(sOd + 3 * NS);
+          T * const sCo = sSo + 3 * NS;
+          if (l < 3)
+            sOd[3 * slot + l] = pick3(X0, l) + toDouble(scl(pick3(sY, l), 0.125f));
+          __syncthreads();
+          if (threadIdx.x < 3 * NS)
+          {
+            T so, co;
+            sinCosPiG(sOd[threadIdx.x], so, co);
+            sSo[threadIdx.x] = so;
+            sCo[threadIdx.x] = co;
+          }
+          __syncthreads();
           T f = cst<T>(1.0);
 #pragma unroll
           for (int d = 0; d < 3; ++d)
-            f = f * sinpiNear(shs(so, g0 + d), shs(co, g0 + d), __shfl_sync(kFull, od, g0 + d), off[d]);
+            f = f * sinpiNear(sSo[3 * slot + d], sCo[3 * slot + d], sOd[3 * slot + d], off[d]);
           rq = adet * (fromDouble<T>(a.rc) * f);
         }
         else
