@@ -125,9 +125,13 @@ pxg_status pxg_create(pxg_ctx ** out, int device)
   c->q1Fp64 = f64 && f64[0] == '1';
   char const * tf64 = getenv("PXG_TET_FP64");
   c->tetFp64 = tf64 && tf64[0] == '1';
+  char const * q2f64 = getenv("PXG_Q2_FP64");
+  c->q2Fp64 = q2f64 && q2f64[0] == '1';
   char const * thr = getenv("PXG_Q1_THREAD");
   c->q1Thread = thr && thr[0] == '1';
   pxg_status s = ensureDevice(c);
+  if (s == PXG_OK && cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    s = cudaFail(c, cudaGetLastError(), "SM count");
   if (s == PXG_OK)
     s = initTables(c);
   if (s == PXG_OK)

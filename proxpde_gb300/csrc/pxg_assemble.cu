@@ -325,6 +325,9 @@ pxg_status initTables(pxg_ctx * c)
       PXG_CUDA(c, cudaMemcpyToSymbol(cQ2xi, xi.data(), xi.size() * 8));
     }
   }
+  pxg_status const q2 = initQ2Tables(c);
+  if (q2 != PXG_OK)
+    return q2;
   if (c->device >= 0 && c->device < 64)
     gTablesDone[c->device] = 1;
   return PXG_OK;
@@ -1248,7 +1251,10 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
         launchAssembleQ1(la, s, c->q1Fp64, c->q1Thread, c->threads);
       break;
     case Q2HEX:
-      launchAssemble<Q2HEX>(la, s, c->threads);
+      if (c->q2Fp64)
+        launchAssemble<Q2HEX>(la, s, c->threads);
+      else
+        launchAssembleQ2(la, s, c->sms);
       break;
     }
   };

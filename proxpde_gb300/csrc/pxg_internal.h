@@ -323,6 +323,8 @@ struct pxg_ctx
   bool q1Generic = false;
   bool q1Fp64 = false;
   bool tetFp64 = false; // P1/P2: the FP64 element kernel instead of kAssembleTet
+  bool q2Fp64 = false;  // Q2: the FP64 element kernel instead of kAssembleQ2
+  int sms = 0;          // SMs of the device (persistent grids)
   bool q1Thread = false;
   CgWork cg;
   AdjState adj;
@@ -452,6 +454,8 @@ pxg_status initTables(pxg_ctx * c);
 // quadrature rule (nodes xi[3 q + d], weights) and shape functions of element type t
 // on the reference element, as proxpde defines them (host)
 void hostRule(int t, std::vector<double> & xi, std::vector<double> & w);
+pxg_status initQ2Tables(pxg_ctx * c);                      // pxg_q2.cu
+void launchAssembleQ2(AsmArgs const & a, cudaStream_t s, int sms); // pxg_q2.cu
 void hostShape(int t, double const * p, double * phi, double * dphi);
 // g_e = -(C u)_e^T K_e (C lambda)_e for every element (pxg_assemble.cu)
 pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, double * g, cudaStream_t s);

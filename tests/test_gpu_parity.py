@@ -236,3 +236,54 @@ def test_tet_two_stiffness_operators(engine):
     for op, mat in zip(ops, g["mats"]):
         csr, _ = O.build(O.P2TET, xyz, conn, em, ndof, lhs=oracle_lhs(op, k))
         compare_csr(mat, csr, ndof)
+
+
+@pytest.mark.parametrize("kernel", ["dfl", "fp64"])
+@pytest.mark.parametrize("n", [3, 5])
+@pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
+@pytest.mark.parametrize("rhs_kind", ["sin3", "projection"])
+def test_q2_kernels_agree_with_oracle(engine, monkeypatch, kernel, n, bc, rhs_kind):
+    """The Q2 kernels against the oracle: the block-per-element double-float kernel
+    (default) and the FP64 element kernel (PXG_Q2_FP64=1); K(k_e) + M with an analytic
+    or a projected load, with and without inhomogeneous Dirichlet data; n = 5 gives
+    more elements than the persistent grid has blocks only on small GPUs, n = 3 fewer."""
+    monkeypatch.setenv("PXG_Q2_FP64", "1" if kernel == "fp64" else "0")
+    xyz, conn, k = problem("hex", n, 0.2, seed=31, sigma=1.0)
+    em, ndof = O.dofmap(O.Q2HEX, xyz.shape[0], conn)
+    dx = O.dof_coords(O.Q2HEX, xyz, conn, em, ndof)
+    ops = [dict(K_OP), {"mass": 1, "mass_coef": 0.75}]
+    field = np.sin(dx[:, 0] + 2 * dx[:, 1]) + dx[:, 2]
+    if rhs_kind == "sin3":
+        rhs = {"kind": 1, "fn": O.FN_SIN3, "coef": 1.5}
+        orhs = {"kind": 1, "fn": O.FN_SIN3, "c": 1.5}
+    else:
+        rhs = {"kind": 2, "fn": 0, "coef": 1.5}
+        orhs = {"kind": 2, "c": 1.5, "field": field}
+    bcarg, mask, val = None, None, None
+    if bc:
+        mask = O.plane_bc_mask(dx, [("y", 0.0), ("z", 1.0)])
+        val = np.where(mask, 0.5 - dx[:, 0], 0.0)
+        dofs = np.nonzero(mask)[0].astype(np.uint32)
+        bcarg = (dofs, val[dofs])
+        ops[0]["apply_bc"] = 1
+        rhs["apply_bc"] = 1
+        orhs["apply_bc"] = 1
+    g = gpu_assemble(O.Q2HEX, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg, field=field)
+    csrK, b = O.build(O.Q2HEX, xyz, conn, em, ndof, lhs=oracle_lhs(ops[0], k), bc_mask=mask, bc_val=val)
+    csrM, _ = O.build(O.Q2HEX, xyz, conn, em, ndof, lhs=oracle_lhs(ops[1], k))
+    _, b = O.build(O.Q2HEX, xyz, conn, em, ndof, rhs=orhs, bc_mask=mask, bc_val=val, b=b)
+    compare_csr(g["mats"][0], csrK, ndof)
+    compare_csr(g["mats"][1], csrM, ndof)
+    assert_close(g["b"], b, what="rhs")
+
+
+def test_q2_two_stiffness_operators(engine):
+    """Q2 with two stiffness operators of different coefficients (no folding into G) and
+    a combined stiffness + mass operator."""
+    xyz, conn, k = problem("hex", 3, 0.2, seed=37, sigma=0.5)
+    em, ndof = O.dofmap(O.Q2HEX, xyz.shape[0], conn)
+    ops = [{"stiffness": 2, "stiff_coef": 0.75, "mass": 1, "mass_coef": 2.0}, {"stiffness": 1, "stiff_coef": 3.0}]
+    g = gpu_assemble(O.Q2HEX, xyz, conn, ops, k=k)
+    for op, mat in zip(ops, g["mats"]):
+        csr, _ = O.build(O.Q2HEX, xyz, conn, em, ndof, lhs=oracle_lhs(op, k))
+        compare_csr(mat, csr, ndof)
