@@ -783,10 +783,10 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
   dfl const kd0 = fromDouble<dfl>(ks0), kd1 = fromDouble<dfl>(ks1);
   dfl const md0 = fromDouble<dfl>(ms0), md1 = fromDouble<dfl>(ms1);
 
-  // --- entries.  Row i is a run-time loop for P2 (a compile-time one for P1); the
-  // columns j are unrolled, so that the element's DOFs and row pointers stay in
-  // registers (a run-time index would move them to local memory, and every entry
-  // would wait on a local load, then on the dependent rowPtr load).
+  // --- entries.  The element's DOFs and row pointers are read with select chains
+  // (pickN): a run-time index into a register array moves it to local memory, and every
+  // entry then waited on a local load and on the dependent rowPtr load.  P1's ten
+  // entries are unrolled.
   int32_t rpn[N];
 #pragma unroll
   for (int n = 0; n < N; ++n)
@@ -800,11 +800,9 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
     uint32_t const dofi = pickN(dof, i);
     int32_t const rpi = pickN(rpn, i);
     bool const ci = (cons >> i) & 1u;
-#pragma unroll
-    for (int j = 0; j < N; ++j)
+#pragma unroll 1
+    for (int j = i; j < N; ++j)
     {
-      if (j < i)
-        continue; // uniform: every thread is in row i
       dfl kv = dfl{0.f, 0.f}, mv = dfl{0.f, 0.f};
       if (needK)
       {
@@ -817,7 +815,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
       if (needM)
         mv = am * MHATd<T>(i, j);
       int32_t const pij = rpi + rk[i * N + j];
-      int32_t const pji = rpn[j] + rk[j * N + i];
+      int32_t const pji = pickN(rpn, j) + rk[j * N + i];
       bool const cj = (cons >> j) & 1u;
 #pragma unroll
       for (int m = 0; m < 2; ++m)
@@ -837,7 +835,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
         double const val = toDouble(v);
         if (anyBc && op.bc && (ci || cj))
         {
-          condenseTet(op.vals + pij, a.bcDiag, a.b, dofi, dof[j], a.bcVal, ci, cj, i == j, val);
+          condenseTet(op.vals + pij, a.bcDiag, a.b, dofi, pickN(dof, j), a.bcVal, ci, cj, i == j, val);
           continue;
         }
         red(op.vals + pij, val);
@@ -883,6 +881,16 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
   double fq[NQ];
   if (a.rkind == 1)
   {
+    // the vertices again (cache hits): keeping them in registers through the entry
+    // loop cost 24 registers per thread
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+    {
+      uint32_t const id = a.conn[e * 4 + v];
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        X[v][d] = a.xyz[3 * (int64_t)id + d];
+    }
 #pragma unroll
     for (int q = 0; q < NQ; ++q)
     {
