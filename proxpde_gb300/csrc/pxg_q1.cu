@@ -981,12 +981,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   if (!lhs)
     return; // uniform over the block: the kernel arguments
 
-  // ---- B. tables, lane l = job l
+  // ---- B. tables: warp w takes job w / SW for the 32 slots 32 (w % SW) + lane, so that
+  // the job is uniform over the warp (the sum jobs skip the U jobs' second transform
+  // and fourth row)
   __syncthreads(); // G of every slot is written
   {
-    uint32_t const code = (uint32_t)((l < 4 ? kJobsLo : kJobsHi) >> (16 * (l & 3))) & 0x7ffu;
+    int const job = (threadIdx.x >> 5) / SW;
+    int const sB = 32 * ((threadIdx.x >> 5) % SW) + (threadIdx.x & 31);
+    uint32_t const code = (uint32_t)((job < 4 ? kJobsLo : kJobsHi) >> (16 * (job & 3))) & 0x7ffu;
     int const cmp = code & 7, su = 1 << ((code >> 3) & 3), sv = 1 << ((code >> 5) & 3), sw3 = 1 << ((code >> 7) & 3);
     int const kind = code >> 9;
+    T const * const Gs = tab + sB * kGStride;
     T F[2][2][2]; // [qw][qv][qu]
 #pragma unroll
     for (int qw = 0; qw < 2; ++qw)
@@ -994,43 +999,60 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       for (int qv = 0; qv < 2; ++qv)
 #pragma unroll
         for (int qu = 0; qu < 2; ++qu)
-          F[qw][qv][qu] = G[cmp * 8 + qu * su + qv * sv + qw * sw3];
+          F[qw][qv][qu] = Gs[cmp * 8 + qu * su + qv * sv + qw * sw3];
     __syncthreads(); // the tables overwrite G
     // constants of the class formulas, evaluated at compile time
-    constexpr T kOne = cst<T>(1.0), kMinusOne = cst<T>(-1.0), kZero = cst<T>(0.0);
     constexpr T kA = cst<T>(A), kB = cst<T>(B), kAA = cst<T>(AA), kBB = cst<T>(BB), kAB = cst<T>(AB);
-    bool const isU = kind == 2;
-    T const a0 = isU ? kA : kOne;
-    T const a1 = isU ? kB : (kind == 1 ? kMinusOne : kOne);
-    T P0[2][2], P1[2][2]; // [qw][qv]: along u with (a0, a1), and with l_1 (U jobs)
-#pragma unroll
-    for (int qw = 0; qw < 2; ++qw)
-#pragma unroll
-      for (int qv = 0; qv < 2; ++qv)
-      {
-        P0[qw][qv] = dot2(a0, F[qw][qv][0], a1, F[qw][qv][1]);
-        P1[qw][qv] = dot2(kB, F[qw][qv][0], kA, F[qw][qv][1]);
-      }
-    // row r along v: classes W_r (sum jobs, r < 3) or l_(r & 1) of P0 / P1 (U jobs)
-    constexpr T kS0[4] = {kAA, kBB, kAB, kZero}, kS1[4] = {kBB, kAA, kAB, kZero};
-    T * const tj = tab + l * 12 * kRow + slot;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
+    T * const tj = tab + job * 12 * kRow + sB;
+    if (kind == 2)
     {
-      T const x0 = isU ? ((r & 1) ? kB : kA) : kS0[r];
-      T const x1 = isU ? ((r & 1) ? kA : kB) : kS1[r];
-      T R[2];
+      // U jobs: along u with l_0 (P0) and l_1 (P1); row r along v: l_(r & 1) of P0 (r < 2)
+      // or of P1 (r >= 2)
+      T P0[2][2], P1[2][2]; // [qw][qv]
 #pragma unroll
       for (int qw = 0; qw < 2; ++qw)
+#pragma unroll
+        for (int qv = 0; qv < 2; ++qv)
+        {
+          P0[qw][qv] = dot2(kA, F[qw][qv][0], kB, F[qw][qv][1]);
+          P1[qw][qv] = dot2(kB, F[qw][qv][0], kA, F[qw][qv][1]);
+        }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
       {
-        T const s0 = (r >= 2 && isU) ? P1[qw][0] : P0[qw][0];
-        T const s1 = (r >= 2 && isU) ? P1[qw][1] : P0[qw][1];
-        R[qw] = dot2(x0, s0, x1, s1);
+        T const x0 = (r & 1) ? kB : kA, x1 = (r & 1) ? kA : kB;
+        T R[2];
+#pragma unroll
+        for (int qw = 0; qw < 2; ++qw)
+          R[qw] = r >= 2 ? dot2(x0, P1[qw][0], x1, P1[qw][1]) : dot2(x0, P0[qw][0], x1, P0[qw][1]);
+        // classes along w
+        tj[(r * 3 + 0) * kRow] = dot2(kAA, R[0], kBB, R[1]);
+        tj[(r * 3 + 1) * kRow] = dot2(kBB, R[0], kAA, R[1]);
+        tj[(r * 3 + 2) * kRow] = kAB * (R[0] + R[1]);
       }
-      // classes along w
-      tj[(r * 3 + 0) * kRow] = dot2(kAA, R[0], kBB, R[1]);
-      tj[(r * 3 + 1) * kRow] = dot2(kBB, R[0], kAA, R[1]);
-      tj[(r * 3 + 2) * kRow] = kAB * (R[0] + R[1]);
+    }
+    else
+    {
+      // sum jobs: along u the sum (kind 0) or the alternating sum (kind 1); row r along v:
+      // the classes W_r (AA, BB), (BB, AA), (AB, AB)
+      T P0[2][2];
+#pragma unroll
+      for (int qw = 0; qw < 2; ++qw)
+#pragma unroll
+        for (int qv = 0; qv < 2; ++qv)
+          P0[qw][qv] = kind == 1 ? F[qw][qv][0] - F[qw][qv][1] : F[qw][qv][0] + F[qw][qv][1];
+      constexpr T kS0[3] = {kAA, kBB, kAB}, kS1[3] = {kBB, kAA, kAB};
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+      {
+        T R[2];
+#pragma unroll
+        for (int qw = 0; qw < 2; ++qw)
+          R[qw] = r == 2 ? kAB * (P0[qw][0] + P0[qw][1]) : dot2(kS0[r], P0[qw][0], kS1[r], P0[qw][1]);
+        tj[(r * 3 + 0) * kRow] = dot2(kAA, R[0], kBB, R[1]);
+        tj[(r * 3 + 1) * kRow] = dot2(kBB, R[0], kAA, R[1]);
+        tj[(r * 3 + 2) * kRow] = kAB * (R[0] + R[1]);
+      }
     }
   }
   __syncthreads();
