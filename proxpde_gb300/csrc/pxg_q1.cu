@@ -693,7 +693,8 @@ struct Smem
   // phase D's scratch (centroid coordinates, their sin and cos) behind G in the table
   // region, which the tables overwrite only in phase B
   static constexpr size_t scratchOff = (size_t)NS * kGStride * 8;
-  static_assert(scratchOff + (size_t)NS * 3 * 24 <= tabBytes, "phase D scratch overlaps the next region");
+  // [NS][3] centroid coordinates, [NS][3] sin, [NS][3] cos, then [NS][8][3] vertex coordinates
+  static_assert(scratchOff + (size_t)NS * (3 * 24 + 24 * 8) <= tabBytes, "phase D scratch overlaps the next region");
   static constexpr size_t slotOff = (tabBytes + 15) / 16 * 16;
   static constexpr size_t bvOff = slotOff + ((size_t)NS * kSlotWords * 4 + 15) / 16 * 16;
   static constexpr size_t bytes = bvOff + (size_t)NS * kBvStride * 8;
@@ -802,6 +803,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   T * const tab = reinterpret_cast<T *>(smem);
   uint32_t * const slotw = reinterpret_cast<uint32_t *>(smem + S::slotOff);
   double * const bvAll = reinterpret_cast<double *>(smem + S::bvOff);
+  // phase D scratch behind G (the tables overwrite it only in phase B)
+  double * const sOd = reinterpret_cast<double *>(smem + S::scratchOff); // [NS][3]
+  T * const sSo = reinterpret_cast<T *>(sOd + 3 * NS);
+  T * const sCo = sSo + 3 * NS;
+  double * const sXv = reinterpret_cast<double *>(sCo + 3 * NS); // [NS][8][3]
 
   int const l = threadIdx.x & 7;
   int const g0 = threadIdx.x & 24; // first lane of the group in the warp
@@ -844,6 +850,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
     double const x = a.xyz[3 * (int64_t)vtx + d];
     X0[d] = __shfl_sync(kFull, x, g0);
     Y[d] = fromDouble<T>(x - X0[d]);
+    sXv[(8 * slot + (l ^ by)) * 3 + d] = x; // node order, for the vertex average (phase D)
   }
   __syncthreads();
 
@@ -920,32 +927,25 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       T rq;
       if (a.rkind == 1)
       {
-        T sY[3]; // sums of the relative coordinates: centroid = X0 + sY / 8
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
+        // the centroid (the vertex average, the hexahedron's origin) and, for the sin
+        // load, sin and cos of pi times its coordinates: one thread per (element,
+        // coordinate) of the block, through shared memory behind G
+        if (threadIdx.x < 3 * NS)
         {
-          T v = Y[d] + shx(Y[d], 1);
-          v = v + shx(v, 2);
-          sY[d] = v + shx(v, 4);
-        }
-        if (a.fn == PXG_FN_SIN3)
-        {
-          // sin and cos of pi times the centroid's coordinates: one thread per
-          // (element, coordinate) of the block, through shared memory behind G
-          double * const sOd = reinterpret_cast<double *>(smem + S::scratchOff); // [NS][3]
-          T * const sSo = reinterpret_cast<T *>(sOd + 3 * NS);
-          T * const sCo = sSo + 3 * NS;
-          if (l < 3)
-            sOd[3 * slot + l] = pick3(X0, l) + toDouble(scl(pick3(sY, l), 0.125f));
-          __syncthreads();
-          if (threadIdx.x < 3 * NS)
+          double const * xv = sXv + 24 * (threadIdx.x / 3) + threadIdx.x % 3;
+          double const od = 0.125 * (xv[0] + xv[3] + xv[6] + xv[9] + xv[12] + xv[15] + xv[18] + xv[21]);
+          sOd[threadIdx.x] = od;
+          if (a.fn == PXG_FN_SIN3)
           {
             T so, co;
-            sinCosPiG(sOd[threadIdx.x], so, co);
+            sinCosPiG(od, so, co);
             sSo[threadIdx.x] = so;
             sCo[threadIdx.x] = co;
           }
-          __syncthreads();
+        }
+        __syncthreads();
+        if (a.fn == PXG_FN_SIN3)
+        {
           T f = cst<T>(1.0);
 #pragma unroll
           for (int d = 0; d < 3; ++d)
@@ -957,7 +957,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
           double x[3];
 #pragma unroll
           for (int d = 0; d < 3; ++d)
-            x[d] = X0[d] + toDouble(scl(sY[d], 0.125f)) + toDouble(off[d]);
+            x[d] = sOd[3 * slot + d] + toDouble(off[d]);
           rq = fromDouble<T>(toDouble(adet) * evalFn(a.fn, a.rc, x[0], x[1], x[2]));
         }
       }
