@@ -678,7 +678,8 @@ constexpr uint64_t kJobsHi = jobc(6, 0, 1, 2, 1) | jobc(3, 0, 1, 2, 2) << 16 | j
 //         slot holds G_xx, G_yy, G_zz, G_xy, G_xz, G_yz and |det J| at its 8 Gauss points
 //   slotw uint32_t[NS][kSlotWords]: rowPtr of the nodes' DOFs, the DOFs, the 8 x 8
 //         scatter ranks (uint16) and the mask of constrained nodes
-//   bv    double[NS][kBvStride]: Dirichlet value of each node (0 when free)
+//   bv    double[NS][kBvStride]: Dirichlet value of each node (0 when free), then k_e
+//   desc  uint4[36][6]: the pair descriptors of phase C (a copy of kPairs32 / kPairs64)
 // The slot strides are odd multiples of the access width, so that the lane-per-slot
 // reads of phase C, and the group-per-slot accesses of the other phases, spread over
 // the banks.
@@ -697,7 +698,8 @@ struct Smem
   static_assert(scratchOff + (size_t)NS * (3 * 24 + 24 * 8) <= tabBytes, "phase D scratch overlaps the next region");
   static constexpr size_t slotOff = (tabBytes + 15) / 16 * 16;
   static constexpr size_t bvOff = slotOff + ((size_t)NS * kSlotWords * 4 + 15) / 16 * 16;
-  static constexpr size_t bytes = bvOff + (size_t)NS * kBvStride * 8;
+  static constexpr size_t descOff = (bvOff + (size_t)NS * kBvStride * 8 + 15) / 16 * 16;
+  static constexpr size_t bytes = descOff + 36 * 6 * 16;
 };
 template <int NT>
 constexpr size_t smemBytes()
@@ -808,6 +810,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   T * const sSo = reinterpret_cast<T *>(sOd + 3 * NS);
   T * const sCo = sSo + 3 * NS;
   double * const sXv = reinterpret_cast<double *>(sCo + 3 * NS); // [NS][8][3]
+  // the pair descriptors of phase C, copied once per block: shared-memory reads
+  // wait less than the L1 hits of the global table
+  uint4 * const sDesc = reinterpret_cast<uint4 *>(smem + S::descOff);
+  {
+    uint4 const * const src = reinterpret_cast<uint4 const *>(NS == 32 ? kPairs32.w : kPairs64.w);
+    for (int k = threadIdx.x; k < 36 * 6; k += NT)
+      sDesc[k] = src[k];
+  }
 
   int const l = threadIdx.x & 7;
   int const g0 = threadIdx.x & 24; // first lane of the group in the warp
@@ -829,7 +839,12 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   sw[kSwDof + l] = dofl;
   bv[l] = bvl;
   if (l == 0)
+  {
     sw[kSwCons] = cons;
+    // the element's coefficient for phase C, in the slot's spare ninth word of bv
+    bool const needKE = (a.op[0].on && a.op[0].stiff == 2) || (a.op[1].on && a.op[1].stiff == 2);
+    bv[8] = (needKE && a.kE) ? a.kE[e] : 1.0;
+  }
   if (lhs)
   {
     sw[kSwRp + l] = a.rowPtr[dofl];
@@ -1064,8 +1079,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   bool const liveS = gs < a.nelem;
   bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
   bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
-  bool const needKE = (a.op[0].on && a.op[0].stiff == 2) || (a.op[1].on && a.op[1].stiff == 2);
-  double const kfac = (needKE && a.kE) ? a.kE[elemOf(a, liveS ? gs : a.nelem - 1)] : 1.0;
+  double const kfac = bvAll[s * kBvStride + 8]; // k_e of slot s (1 without a per-element coefficient)
   // operator coefficients in the arithmetic of the tables: the only FP64 instruction
   // of an entry is then the addition in its conversion to double (the FP64 pipe, at
   // 1/64 of the FP32 rate, is the scarcer resource)
@@ -1083,11 +1097,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   bool const anyBcS = consS && ((a.op[0].on && a.op[0].bc) || (a.op[1].on && a.op[1].bc));
   char const * const col = reinterpret_cast<char const *>(tab + s);
   char const * const rk = reinterpret_cast<char const *>(ss + kSwRank);
-  uint4 const * const pt = reinterpret_cast<uint4 const *>(NS == 32 ? kPairs32.w : kPairs64.w);
+  uint4 const * const pt = sDesc;
   for (int p = warp / SW; p < 36; p += 8)
   {
-    uint4 const d0 = __ldg(pt + 6 * p), d1 = __ldg(pt + 6 * p + 1), d2 = __ldg(pt + 6 * p + 2);
-    uint4 const d3 = __ldg(pt + 6 * p + 3), d4 = __ldg(pt + 6 * p + 4), d5 = __ldg(pt + 6 * p + 5);
+    uint4 const d0 = pt[6 * p], d1 = pt[6 * p + 1], d2 = pt[6 * p + 2];
+    uint4 const d3 = pt[6 * p + 3], d4 = pt[6 * p + 4], d5 = pt[6 * p + 5];
     T kv = cst<T>(0.0), mv = cst<T>(0.0);
     if (needK)
     {
