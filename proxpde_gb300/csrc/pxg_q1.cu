@@ -109,7 +109,7 @@ __device__ __forceinline__ double sinpiNear(double so, double co, double o, doub
 // The same in double-float.  For |u| < 0.05 the terms u^4/120 (< 6e-8) and beyond,
 // and u^4/24 (< 3e-7) and beyond, are needed to 1e-14 absolute only, which float
 // arithmetic gives; u^2/6 and u^2/2 are kept in double-float.
-__device__ __forceinline__ dfl sinpiNear(dfl so, dfl co, double o, dfl d)
+__device__ __noinline__ dfl sinpiNear(dfl so, dfl co, double o, dfl d)
 {
   dfl const u = cst<dfl>(PI) * d;
   if (fabsf(u.h) < 0.05f)
@@ -624,10 +624,12 @@ __device__ __forceinline__ T lerp2(T v, int m)
   return dot2(cst<T>(A), v, cst<T>(B), shx(v, m));
 }
 
+// Out of line, like sinpiNear: a smaller instruction footprint for the phases of the
+// group kernel (measured 0.8 % faster at 128^3).
 // sin(pi o), cos(pi o): o = k/2 + r with |r| <= 1/4 (exact in FP64; adding 1.5 * 2^52
 // rounds 2o to an integer), Taylor polynomials of sin and cos at x = pi r with the
 // terms above 2^-24 in double-float and the rest in float, then the quadrant k mod 4.
-__device__ __forceinline__ void sinCosPiG(double o, dfl & s, dfl & c)
+__device__ __noinline__ void sinCosPiG(double o, dfl & s, dfl & c)
 {
   constexpr double kRound = 6755399441055744.0;
   double const kk = fma(2.0, o, kRound);
