@@ -40,7 +40,7 @@ typedef enum pxg_status
   PXG_ERR_NOT_CONVERGED = 5, /* an iterative solve stopped at its iteration limit */
   PXG_ERR_UNSUPPORTED = 6,   /* element type / operator combination not provided */
   PXG_ERR_NO_DEVICE = 7,     /* no CUDA device, or the requested one is absent */
-  PXG_ERR_NUMERIC = 8        /* a degenerate element (zero Jacobian) or a NaN input */
+  PXG_ERR_NUMERIC = 8        /* a device procedure did not finish (the element colouring) */
 } pxg_status;
 
 /* Element types: LagrangeFE<Tetrahedron,1|2>, LagrangeFE<Hexahedron,1|2> with their
