@@ -1130,24 +1130,47 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
     uint32_t const pij = ss[kSwRp + i] + *reinterpret_cast<uint16_t const *>(rk + (d5.z & 0xffffu));
     uint32_t const pji = ss[kSwRp + j] + *reinterpret_cast<uint16_t const *>(rk + (d5.z >> 16));
     bool const ci = (consS >> i) & 1u, cj = (consS >> j) & 1u;
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
+    // a warp none of whose elements has a constrained node in this pair takes the path
+    // without the Dirichlet checks (every warp of a problem without BCs)
+    bool const bcHere = anyBcS && (ci || cj);
+    if (__any_sync(kFull, bcHere))
     {
-      LhsDev const & op = a.op[m];
-      if (!op.on)
-        continue;
-      double const val = toDouble(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
-      if (!liveS)
-        continue;
-      if (anyBcS && op.bc && (ci || cj))
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
       {
-        condenseEntry(op.vals + pij, a.bcDiag, a.b, ss[kSwDof + i], ss[kSwDof + j], bs[i], bs[j], ci, cj, i == j,
-                      val);
-        continue;
+        LhsDev const & op = a.op[m];
+        if (!op.on)
+          continue;
+        double const val = toDouble(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
+        if (!liveS)
+          continue;
+        if (bcHere && op.bc)
+        {
+          condenseEntry(op.vals + pij, a.bcDiag, a.b, ss[kSwDof + i], ss[kSwDof + j], bs[i], bs[j], ci, cj, i == j,
+                        val);
+          continue;
+        }
+        atomicAdd(op.vals + pij, val);
+        if (i != j)
+          atomicAdd(op.vals + pji, val);
       }
-      atomicAdd(op.vals + pij, val);
-      if (i != j)
-        atomicAdd(op.vals + pji, val);
+    }
+    else
+    {
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+      {
+        LhsDev const & op = a.op[m];
+        if (!op.on)
+          continue;
+        double const val = toDouble(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
+        if (liveS)
+        {
+          atomicAdd(op.vals + pij, val);
+          if (i != j)
+            atomicAdd(op.vals + pji, val);
+        }
+      }
     }
   }
 }
