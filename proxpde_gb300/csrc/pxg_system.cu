@@ -73,6 +73,7 @@ struct SysArgs
   int nops;
   int kind[4];
   double coef[4];
+  int pairPath; // one space, stiffness / tensor stiffness / mass only: the block path
   int32_t const * rowPtr;
   int32_t const * colIdx;
   double * vals;
@@ -93,6 +94,31 @@ __device__ __forceinline__ int64_t position(int32_t const * rp, int32_t const * 
   return lo;
 }
 
+// Entry (I, J) = (row DOF i, component d1; column DOF j, component d2) of element e:
+// the call's Dirichlet condensation, or the FP64 reduction at its CSR position
+__device__ __forceinline__ void sysEmit(SysArgs const & a, int64_t e, int I, int J, double v,
+                                       unsigned char const * consR, unsigned char const * consC, double const * h)
+{
+  int const i = I % a.Nr, d1 = I / a.Nr, j = J % a.Nc, d2 = J / a.Nc;
+  int64_t const gI = a.offr + a.emr[e * a.Nr + i] + (int64_t)d1 * a.ndr;
+  int64_t const gJ = a.offc + a.emc[e * a.Nc + j] + (int64_t)d2 * a.ndc;
+  bool const cI = consR[I], cJ = consC[J];
+  if (cI || cJ)
+  {
+    if (!cI && a.b && h[J] != 0.)
+      atomicAdd(a.b + gI, -v * h[J]); // lift: Fe = -C Ke h
+    if (a.diagCall && I == J)
+    {
+      // buildLhs: constrained diagonal = diag, Fe = h (builder.hpp:105-124)
+      atomicAdd(a.vals + position(a.rowPtr, a.colIdx, gI, (int32_t)gI), a.diag);
+      if (a.b)
+        atomicAdd(a.b + gI, h[J]);
+    }
+    return;
+  }
+  atomicAdd(a.vals + position(a.rowPtr, a.colIdx, gI, (int32_t)gJ), v);
+}
+
 __global__ void __launch_bounds__(kSysThreads) kSysAssemble(SysArgs a)
 {
   extern __shared__ double sm[];
@@ -103,7 +129,8 @@ __global__ void __launch_bounds__(kSysThreads) kSysAssemble(SysArgs a)
   double * dRr = JxW + nq;          // nq * Nr * 3
   double * dRc = dRr + nq * Nr * 3; // nq * Nc * 3
   double * h = dRc + nq * Nc * 3;   // Lc
-  auto * consR = reinterpret_cast<unsigned char *>(h + Lc);
+  double * wph = h + Lc;            // nq * Nr: JxW phi (block path)
+  auto * consR = reinterpret_cast<unsigned char *>(wph + nq * Nr);
   unsigned char * consC = consR + Lr;
   double const * W = a.tab;
   double const * dV = W + nq;
@@ -169,6 +196,85 @@ __global__ void __launch_bounds__(kSysThreads) kSysAssemble(SysArgs a)
       h[J] = cj ? a.valc[id] : 0.;
     }
     __syncthreads();
+    if (a.pairPath)
+    {
+      // one space: B_d1d2(i, j) = sum_q JxW grad_d1 phi_i grad_d2 phi_j for the pairs
+      // i <= j gives all nine component blocks of (i, j) and, transposed, of (j, i); the
+      // stiffness is the trace of B
+      for (int k = threadIdx.x; k < nq * Nr; k += blockDim.x)
+      {
+        double const w = JxW[k / Nr];
+        dRc[3 * k] = w * dRr[3 * k];
+        dRc[3 * k + 1] = w * dRr[3 * k + 1];
+        dRc[3 * k + 2] = w * dRr[3 * k + 2];
+        wph[k] = w * phr[k];
+      }
+      __syncthreads();
+      bool needM = false;
+      for (int k = 0; k < a.nops; ++k)
+        needM = needM || a.kind[k] == PXG_OP_MASS;
+      for (int p = threadIdx.x; p < Nr * (Nr + 1) / 2; p += blockDim.x)
+      {
+        int i = 0, rem = p;
+        while (rem >= Nr - i)
+        {
+          rem -= Nr - i;
+          ++i;
+        }
+        int const j = i + rem;
+        double B[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}}, M = 0.;
+        for (int q = 0; q < nq; ++q)
+        {
+          double const * gi = dRr + 3 * (q * Nr + i);
+          double const * wj = dRc + 3 * (q * Nr + j);
+#pragma unroll
+          for (int d1 = 0; d1 < 3; ++d1)
+#pragma unroll
+            for (int d2 = 0; d2 < 3; ++d2)
+              B[d1][d2] = fma(gi[d1], wj[d2], B[d1][d2]);
+          if (needM)
+            M = fma(phr[q * Nr + i], wph[q * Nr + j], M);
+        }
+        double const K = B[0][0] + B[1][1] + B[2][2];
+        for (int d1 = 0; d1 < a.dr; ++d1)
+          for (int d2 = 0; d2 < a.dr; ++d2)
+          {
+            double v = 0., vt = 0.; // entries (i d1, j d2) and (j d1, i d2)
+            for (int k = 0; k < a.nops; ++k)
+            {
+              double const c = a.coef[k];
+              switch (a.kind[k])
+              {
+              case PXG_OP_STIFFNESS:
+                if (d1 == d2)
+                {
+                  v += c * K;
+                  vt += c * K;
+                }
+                break;
+              case PXG_OP_TENSOR_STIFFNESS:
+              {
+                double const dk = d1 == d2 ? K : 0.;
+                v += c * (dk + B[d1][d2]);
+                vt += c * (dk + B[d2][d1]);
+                break;
+              }
+              case PXG_OP_MASS:
+                if (d1 == d2)
+                {
+                  v += c * M;
+                  vt += c * M;
+                }
+                break;
+              }
+            }
+            sysEmit(a, e, d1 * Nr + i, d2 * Nr + j, v, consR, consC, h);
+            if (i != j)
+              sysEmit(a, e, d1 * Nr + j, d2 * Nr + i, vt, consR, consC, h);
+          }
+      }
+      continue;
+    }
     for (int p = threadIdx.x; p < Lr * Lc; p += blockDim.x)
     {
       int const I = p / Lc, J = p % Lc;
@@ -207,23 +313,7 @@ __global__ void __launch_bounds__(kSysThreads) kSysAssemble(SysArgs a)
         }
         v += a.coef[k] * s;
       }
-      int64_t const gI = a.offr + a.emr[e * Nr + i] + (int64_t)d1 * a.ndr;
-      int64_t const gJ = a.offc + a.emc[e * Nc + j] + (int64_t)d2 * a.ndc;
-      bool const cI = consR[I], cJ = consC[J];
-      if (cI || cJ)
-      {
-        if (!cI && a.b && h[J] != 0.)
-          atomicAdd(a.b + gI, -v * h[J]); // lift: Fe = -C Ke h
-        if (a.diagCall && I == J)
-        {
-          // buildLhs: constrained diagonal = diag, Fe = h (builder.hpp:105-124)
-          atomicAdd(a.vals + position(a.rowPtr, a.colIdx, gI, (int32_t)gI), a.diag);
-          if (a.b)
-            atomicAdd(a.b + gI, h[J]);
-        }
-        continue;
-      }
-      atomicAdd(a.vals + position(a.rowPtr, a.colIdx, gI, (int32_t)gJ), v);
+      sysEmit(a, e, I, J, v, consR, consC, h);
     }
   }
 }
@@ -539,8 +629,13 @@ pxg_status pxg_sys_assemble(pxg_sys * s, int row, int col, int const * kinds, do
   a.colIdx = s->colIdx.p;
   a.vals = vals;
   a.b = b;
+  a.pairPath = row == col;
+  for (int k = 0; k < nops; ++k)
+    a.pairPath = a.pairPath && (kinds[k] == PXG_OP_STIFFNESS || kinds[k] == PXG_OP_TENSOR_STIFFNESS ||
+                                kinds[k] == PXG_OP_MASS);
   int const Lr = Nr * a.dr, Lc = Nc * a.dc;
-  size_t const smem = (24 + 10 * (size_t)a.nq + 3 * (size_t)a.nq * (Nr + Nc) + Lc) * 8 + Lr + Lc;
+  size_t const smem =
+      (24 + 10 * (size_t)a.nq + 3 * (size_t)a.nq * (Nr + Nc) + Lc + (size_t)a.nq * Nr) * 8 + Lr + Lc;
   unsigned const grid = (unsigned)std::min<int64_t>(a.nelem, 152 * 8);
   kSysAssemble<<<grid, kSysThreads, smem, st0>>>(a);
   PXG_CUDA(cr, cudaGetLastError());
