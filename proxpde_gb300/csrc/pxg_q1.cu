@@ -580,12 +580,13 @@ namespace q1g
 {
 using namespace q1;
 
-// Threads per block (default; 128 and 512 are the other candidates of the autotuner).
+// Threads per block (default; 512 is the autotuner's other candidate: the entry phase
+// takes a warp of element slots at a time, so a block holds at least 32 elements).
 // The phases end at block barriers: the warps of a block then run the same phase, and
 // the SM's instruction cache holds the code of a few phases only (one per resident
-// block).  Measured at 128^3 (ms per launch): 128 threads with warp-level syncs 3.11,
-// 128 / 256 / 512 / 1024 threads with block barriers 3.03 / 2.77 / 3.09 / 3.40; 256
-// threads at 80 registers 2.99.
+// block).  Measured at 128^3 on an earlier form of the kernel (ms per launch): 128
+// threads with warp-level syncs 3.11, 128 / 256 / 512 / 1024 threads with block
+// barriers 3.03 / 2.77 / 3.09 / 3.40; 256 threads at 80 registers 2.99.
 constexpr int kThreads = 256;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kAlpha01 = 0.5 * (AA + BB), kBeta0 = 0.5 * (AA - BB);
@@ -693,8 +694,8 @@ struct Smem
 {
   static constexpr int NS = NT / 8, kRow = NS + 1;
   static constexpr size_t tabBytes = (size_t)(96 * kRow > NS * kGStride ? 96 * kRow : NS * kGStride) * 8;
-  // phase D's scratch (centroid coordinates, their sin and cos) behind G in the table
-  // region, which the tables overwrite only in phase B
+  // the scratch of phases 0 and D (vertex and centroid coordinates, the centroid's sin
+  // and cos) behind G in the table region, which the tables overwrite only in phase B
   static constexpr size_t scratchOff = (size_t)NS * kGStride * 8;
   // [NS][3] centroid coordinates, [NS][3] sin, [NS][3] cos, then [NS][8][3] vertex coordinates
   static_assert(scratchOff + (size_t)NS * (3 * 24 + 24 * 8) <= tabBytes, "phase D scratch overlaps the next region");
