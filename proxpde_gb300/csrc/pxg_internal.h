@@ -422,8 +422,10 @@ __device__ __forceinline__ double rowDot(int32_t const * __restrict__ rp, int32_
       {
         int32_t const k = base + u * LPR;
         bool const ok = k < e;
-        cc[u] = ok ? ci[k] : -1;
-        av[u] = ok ? a[k] : 0.;
+        // the matrix is streamed once per product: evict-first loads, so that it does not
+        // push the gathered vector out of L2
+        cc[u] = ok ? __ldcs(ci + k) : -1;
+        av[u] = ok ? __ldcs(a + k) : 0.;
       }
 #pragma unroll
       for (int u = 0; u < UNR; ++u)
