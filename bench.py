@@ -564,7 +564,10 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded perturbed cube)",
+            "vs_baseline": None, "dtype": "f32x2+f64",
+            "arithmetic": "double-float (unevaluated f32 pairs, ~48-bit significand) on the FP32 pipes; FP64 for "
+                          "the coordinate differences, the final hi+lo sums and the reductions; f64 outputs",
+            "data": "synthetic (seeded perturbed cube)",
             "config": {"workload": f"q1hex perturbed {n}^3: K(k_e)+M+rhs sin3, fused pass + prune check",
                        "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned), "tuning": tuning,
                        "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
