@@ -204,10 +204,12 @@ class Context:
 
     # --- inputs
     def set_mesh(self, etype, xyz, conn):
-        self.etype = etype
-        self.nelem = int(conn.shape[0])
-        self._check(self.L.pxg_set_mesh(self.h, etype, _ptr(xyz), int(xyz.shape[0]), _ptr(conn), self.nelem,
+        nelem = int(conn.shape[0])
+        self._check(self.L.pxg_set_mesh(self.h, etype, _ptr(xyz), int(xyz.shape[0]), _ptr(conn), nelem,
                                         _mem(xyz)), "set_mesh")
+        # recorded once the library accepted the mesh
+        self.etype = etype
+        self.nelem = nelem
 
     def set_coords(self, xyz, stream=None):
         self._check(self.L.pxg_set_coords(self.h, _ptr(xyz), _mem(xyz), stream), "set_coords")

@@ -1083,9 +1083,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   bool const needK = (a.op[0].on && a.op[0].stiff) || (a.op[1].on && a.op[1].stiff);
   bool const needM = (a.op[0].on && a.op[0].mass) || (a.op[1].on && a.op[1].mass);
   double const kfac = bvAll[s * kBvStride + 8]; // k_e of slot s (1 without a per-element coefficient)
-  // operator coefficients in the arithmetic of the tables: the only FP64 instruction
-  // of an entry is then the addition in its conversion to double (the FP64 pipe, at
-  // 1/64 of the FP32 rate, is the scarcer resource)
+  // operator coefficients in the arithmetic of the tables: the only FP64-pipe
+  // instructions of an entry are then its conversion to double, the high float's
+  // hardware conversion and the addition of the low float (toDoubleMixed; the FP64
+  // pipe, at 1/64 of the FP32 rate, is the scarcer resource)
   T ks[2], ms[2];
 #pragma unroll
   for (int m = 0; m < 2; ++m)
@@ -1142,7 +1143,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
         LhsDev const & op = a.op[m];
         if (!op.on)
           continue;
-        double const val = toDouble(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
+        double const val = toDoubleMixed(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
         if (!liveS)
           continue;
         if (bcHere && op.bc)
@@ -1164,7 +1165,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
         LhsDev const & op = a.op[m];
         if (!op.on)
           continue;
-        double const val = toDouble(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
+        double const val = toDoubleMixed(op.stiff ? (op.mass ? dot2(ks[m], kv, ms[m], mv) : ks[m] * kv) : ms[m] * mv);
         if (liveS)
         {
           atomicAdd(op.vals + pij, val);

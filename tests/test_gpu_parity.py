@@ -134,6 +134,9 @@ def test_invalid_inputs_rejected(engine):
     assert ei.value.status == 1
     with pytest.raises(PxgError):
         ctx.set_mesh(7, xyz, conn)  # unknown element type
+    with pytest.raises(PxgError) as ei:
+        ctx.set_mesh(O.Q1HEX, xyz, conn[:0])  # no elements
+    assert ei.value.status == 1
     ctx.set_mesh(O.Q1HEX, xyz, conn)
     with pytest.raises(PxgError):
         ctx.build_pattern()  # before the DOF map
@@ -224,6 +227,22 @@ def test_tet_kernels_agree_with_oracle(engine, monkeypatch, kernel, t, gen, n, b
     compare_csr(g["mats"][0], csrK, ndof)
     compare_csr(g["mats"][1], csrM, ndof)
     assert_close(g["b"], b, what="rhs")
+
+
+@pytest.mark.parametrize("kernel", ["dfl", "fp64"])
+def test_q1_two_stiffness_operators(engine, monkeypatch, kernel):
+    """The Q1 group kernel with two stiffness operators of different coefficients, one
+    of them combined with a mass term of coefficient 2, and with the operators swapped
+    (mass first), on a perturbed mesh with a partly filled last block."""
+    monkeypatch.setenv("PXG_Q1_FP64", "1" if kernel == "fp64" else "0")
+    xyz, conn, k = problem("hex", 7, 0.2, seed=37, sigma=1.0)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    for ops in ([{"stiffness": 2, "stiff_coef": 0.75, "mass": 1, "mass_coef": 2.0}, {"stiffness": 1, "stiff_coef": 3.0}],
+                [{"mass": 1, "mass_coef": 0.3}, {"stiffness": 2, "stiff_coef": 2.5}]):
+        g = gpu_assemble(O.Q1HEX, xyz, conn, ops, k=k)
+        for op, mat in zip(ops, g["mats"]):
+            csr, _ = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs=oracle_lhs(op, k))
+            compare_csr(mat, csr, ndof)
 
 
 def test_tet_two_stiffness_operators(engine):
