@@ -1102,12 +1102,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   char const * const col = reinterpret_cast<char const *>(tab + s);
   char const * const rk = reinterpret_cast<char const *>(ss + kSwRank);
   uint4 const * const pt = sDesc;
-  for (int p = warp / SW; p < 36; p += 8)
-  {
+  // pair p of slot s: the stiffness sum kv (nine table terms), the mass term mv, the
+  // local indices and the positions of entries (i, j) and (j, i) in the value arrays
+  auto pairTerms = [&](int p, bool withK, bool withM, T & kv, T & mv, int & i, int & j, uint32_t & pij,
+                       uint32_t & pji) {
     uint4 const d0 = pt[6 * p], d1 = pt[6 * p + 1], d2 = pt[6 * p + 2];
     uint4 const d3 = pt[6 * p + 3], d4 = pt[6 * p + 4], d5 = pt[6 * p + 5];
-    T kv = cst<T>(0.0), mv = cst<T>(0.0);
-    if (needK)
+    kv = cst<T>(0.0);
+    mv = cst<T>(0.0);
+    if (withK)
     {
       auto acc = sumStartS(ldTab<T>(col, d0.x), d2.y);
       sumAddS(acc, ldTab<T>(col, d0.y), d2.z);
@@ -1120,7 +1123,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       sumAddS(acc, ldTab<T>(col, d2.x), d4.y);
       kv = sumEnd(acc);
     }
-    if (needM)
+    if (withM)
     {
       constexpr T kAB = cst<T>(AB), kA01 = cst<T>(kAlpha01), kB0 = cst<T>(kBeta0), kZero = cst<T>(0.0);
       uint32_t const cx = d5.x;
@@ -1128,9 +1131,45 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
       T const beta = negIf(cx == 2 ? kZero : kB0, cx == 1);
       mv = dot2(alpha, ldTab<T>(col, d4.z), beta, ldTab<T>(col, d4.w));
     }
-    int const i = d5.y & 7, j = d5.y >> 3;
-    uint32_t const pij = ss[kSwRp + i] + *reinterpret_cast<uint16_t const *>(rk + (d5.z & 0xffffu));
-    uint32_t const pji = ss[kSwRp + j] + *reinterpret_cast<uint16_t const *>(rk + (d5.z >> 16));
+    i = d5.y & 7;
+    j = d5.y >> 3;
+    pij = ss[kSwRp + i] + *reinterpret_cast<uint16_t const *>(rk + (d5.z & 0xffffu));
+    pji = ss[kSwRp + j] + *reinterpret_cast<uint16_t const *>(rk + (d5.z >> 16));
+  };
+  // The usual operator pair, a stiffness-only operator and then a mass-only one, in a
+  // warp none of whose 32 elements has a Dirichlet node under an operator with BCs:
+  // a loop without the per-entry operator branches and Dirichlet votes.
+  bool const kmPair = a.op[0].on && a.op[0].stiff && !a.op[0].mass && a.op[1].on && !a.op[1].stiff && a.op[1].mass;
+  if (kmPair && !__any_sync(kFull, anyBcS))
+  {
+    double * const vK = a.op[0].vals;
+    double * const vM = a.op[1].vals;
+    for (int p = warp / SW; p < 36; p += 8)
+    {
+      T kv, mv;
+      int i, j;
+      uint32_t pij, pji;
+      pairTerms(p, true, true, kv, mv, i, j, pij, pji);
+      double const valK = toDoubleMixed(ks[0] * kv), valM = toDoubleMixed(ms[1] * mv);
+      if (liveS)
+      {
+        atomicAdd(vK + pij, valK);
+        atomicAdd(vM + pij, valM);
+        if (i != j)
+        {
+          atomicAdd(vK + pji, valK);
+          atomicAdd(vM + pji, valM);
+        }
+      }
+    }
+    return;
+  }
+  for (int p = warp / SW; p < 36; p += 8)
+  {
+    T kv, mv;
+    int i, j;
+    uint32_t pij, pji;
+    pairTerms(p, needK, needM, kv, mv, i, j, pij, pji);
     bool const ci = (consS >> i) & 1u, cj = (consS >> j) & 1u;
     // a warp none of whose elements has a constrained node in this pair takes the path
     // without the Dirichlet checks (every warp of a problem without BCs)
