@@ -794,53 +794,93 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
   bool const anyBc = cons && ((op0.on && op0.bc) || (op1.on && op1.bc));
   uint16_t const * rk = a.rank + e * (int64_t)(N * N);
   constexpr int kRowUnroll = N <= 4 ? N : 1; // P1: the 10 entries fully unrolled
-#pragma unroll kRowUnroll
-  for (int i = 0; i < N; ++i)
+  // P1 with the usual operator pair, a stiffness-only operator and then a mass-only one
+  // (both coefficients folded above), in a warp none of whose elements has a Dirichlet
+  // node under an operator with BCs: a loop without the per-entry operator branches
+  // (96^3 x 6: 0.78 -> 0.75 ms; for P2 the same loop measured 2 % slower, so P2 keeps
+  // the general one).  The vote runs over the active lanes: the last block's spare
+  // threads have returned.
+  bool fastDone = false;
+  bool const kmPair = op0.on && op0.stiff && !op0.mass && op1.on && !op1.stiff && op1.mass;
+  if constexpr (T == P1TET)
+    fastDone = kmPair && !__any_sync(__activemask(), anyBc);
+  if (fastDone)
   {
-    uint32_t const dofi = pickN(dof, i);
-    int32_t const rpi = pickN(rpn, i);
-    bool const ci = (cons >> i) & 1u;
-#pragma unroll 1
-    for (int j = i; j < N; ++j)
+#pragma unroll kRowUnroll
+    for (int i = 0; i < N; ++i)
     {
-      dfl kv = dfl{0.f, 0.f}, mv = dfl{0.f, 0.f};
-      if (needK)
+      int32_t const rpi = pickN(rpn, i);
+#pragma unroll 1
+      for (int j = i; j < N; ++j)
       {
         dfl t[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k)
           t[k] = TTd<T>(k, i, j);
-        kv = dot6(G, t);
-      }
-      if (needM)
-        mv = am * MHATd<T>(i, j);
-      int32_t const pij = rpi + rk[i * N + j];
-      int32_t const pji = pickN(rpn, j) + rk[j * N + i];
-      bool const cj = (cons >> j) & 1u;
-#pragma unroll
-      for (int m = 0; m < 2; ++m)
-      {
-        LhsDev const & op = a.op[m];
-        if (!op.on)
-          continue;
-        dfl v;
-        if (op.stiff)
-        {
-          v = foldK ? kv : (m ? kd1 : kd0) * kv;
-          if (op.mass)
-            v = v + (foldM ? mv : (m ? md1 : md0) * mv);
-        }
-        else
-          v = foldM ? mv : (m ? md1 : md0) * mv;
-        double const val = toDouble(v);
-        if (anyBc && op.bc && (ci || cj))
-        {
-          condenseTet(op.vals + pij, a.bcDiag, a.b, dofi, pickN(dof, j), a.bcVal, ci, cj, i == j, val);
-          continue;
-        }
-        red(op.vals + pij, val);
+        double const valK = toDouble(dot6(G, t));
+        double const valM = toDouble(am * MHATd<T>(i, j));
+        int32_t const pij = rpi + rk[i * N + j];
+        red(op0.vals + pij, valK);
+        red(op1.vals + pij, valM);
         if (j != i)
-          red(op.vals + pji, val);
+        {
+          int32_t const pji = pickN(rpn, j) + rk[j * N + i];
+          red(op0.vals + pji, valK);
+          red(op1.vals + pji, valM);
+        }
+      }
+    }
+  }
+  else
+  {
+#pragma unroll kRowUnroll
+    for (int i = 0; i < N; ++i)
+    {
+      uint32_t const dofi = pickN(dof, i);
+      int32_t const rpi = pickN(rpn, i);
+      bool const ci = (cons >> i) & 1u;
+#pragma unroll 1
+      for (int j = i; j < N; ++j)
+      {
+        dfl kv = dfl{0.f, 0.f}, mv = dfl{0.f, 0.f};
+        if (needK)
+        {
+          dfl t[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k)
+            t[k] = TTd<T>(k, i, j);
+          kv = dot6(G, t);
+        }
+        if (needM)
+          mv = am * MHATd<T>(i, j);
+        int32_t const pij = rpi + rk[i * N + j];
+        int32_t const pji = pickN(rpn, j) + rk[j * N + i];
+        bool const cj = (cons >> j) & 1u;
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+        {
+          LhsDev const & op = a.op[m];
+          if (!op.on)
+            continue;
+          dfl v;
+          if (op.stiff)
+          {
+            v = foldK ? kv : (m ? kd1 : kd0) * kv;
+            if (op.mass)
+              v = v + (foldM ? mv : (m ? md1 : md0) * mv);
+          }
+          else
+            v = foldM ? mv : (m ? md1 : md0) * mv;
+          double const val = toDouble(v);
+          if (anyBc && op.bc && (ci || cj))
+          {
+            condenseTet(op.vals + pij, a.bcDiag, a.b, dofi, pickN(dof, j), a.bcVal, ci, cj, i == j, val);
+            continue;
+          }
+          red(op.vals + pij, val);
+          if (j != i)
+            red(op.vals + pji, val);
+        }
       }
     }
   }
