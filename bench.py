@@ -116,6 +116,30 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def gpu_local_cpus(dev):
+    """(CPUs of this process that are local to the GPU, the GPU's NUMA node), from the
+    PCI device's sysfs entries; (None, None) where they are not readable. Pinned host
+    buffers are placed on the node of the thread that allocates them, and a host-device
+    copy through a buffer on the far CPU's memory crosses the link between the CPUs."""
+    import torch
+
+    p = torch.cuda.get_device_properties(dev)
+    base = f"/sys/bus/pci/devices/{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+    try:
+        with open(base + "/local_cpulist") as f:
+            spec = f.read().strip()
+        with open(base + "/numa_node") as f:
+            node = int(f.read().strip())
+    except (OSError, ValueError):
+        return None, None
+    cpus = set()
+    for part in spec.split(","):
+        if part:
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+    return cpus & os.sched_getaffinity(0), node
+
+
 def cpu_sample(n_sample, threads):
     """The oracle (restated reference loop: triplets + setFromTriplets + prune) on a
     bounded sample of the same workload; returns elements/s."""
@@ -493,6 +517,12 @@ def main():
         # counts back into pinned memory.  Two output sets alternate, so that the
         # read-back of step i (on a copy stream) overlaps the upload and the assembly
         # of step i + 1.
+        # pinned buffers on the GPU's own CPU node: the allocating and launching thread
+        # runs on the CPUs local to the GPU while they are allocated and used
+        allowed = os.sched_getaffinity(0)
+        local, node = gpu_local_cpus(dev)
+        if local:
+            os.sched_setaffinity(0, local)
         xyz_h = torch.from_numpy(xyz).pin_memory()
         k_h = torch.from_numpy(k).pin_memory()
         copy_stream = torch.cuda.Stream(dev)
@@ -537,9 +567,13 @@ def main():
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t1) / args.steps
         assert all(S["cnth"].tolist() == pruned for S in sets), "prune counts differ between the two legs"
+        os.sched_setaffinity(0, allowed)
         e2e = {"value": world * E / e2e_s, "unit": UNIT, "h2d_bytes_per_step": xyz.nbytes + k.nbytes,
                "d2h_bytes_per_step": 2 * nnz * 8 + ndof * 8 + 16, "ms_per_step": e2e_s * 1e3,
-               "overlap": "read-back of step i overlaps upload and assembly of step i + 1 (two output sets)"}
+               "overlap": "read-back of step i overlaps upload and assembly of step i + 1 (two output sets)",
+               "host": {"gpu_numa_node": node, "cpus_allowed": len(allowed),
+                        "cpus_used": len(local) if local else len(allowed),
+                        "placement": "CPUs local to the GPU" if local else "process affinity unchanged"}}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

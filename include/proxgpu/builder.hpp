@@ -356,22 +356,60 @@ struct AssemblyScalarMass
 template <typename FE>
 using AssemblyMass = AssemblyScalarMass<FE>;
 
+// AssemblyRhsAnalytic(f, feSpace, comps) (include/assembly_rhs.hpp:34-91) with device
+// functions chosen by id.  A scalar space takes one id; a vector space takes one id
+// and one coefficient per component (the components of the reference's vector
+// function), and only the listed components (default: all) get a load, component c
+// into block c.
 template <typename FE>
 struct AssemblyRhsAnalytic
 {
   int fn;
   double coef;
   FE const * feSpace;
-  AssemblyRhsAnalytic(int f, FE const & fe, double c = 1.0): fn(f), coef(c), feSpace(&fe) {}
+  std::vector<int> fns;      // per component
+  std::vector<double> coefs; // per component
+  std::vector<int> comps;
+  AssemblyRhsAnalytic(int f, FE const & fe, double c = 1.0): fn(f), coef(c), feSpace(&fe), fns{f}, coefs{c}, comps{0}
+  {
+    static_assert(FE::dim == 1, "this ctor is available only for scalar fe spaces.");
+  }
+  AssemblyRhsAnalytic(std::array<int, FE::dim> const & f, FE const & fe, std::array<double, FE::dim> const & c,
+                      std::vector<int> cmp = {}):
+      fn(f[0]), coef(c[0]), feSpace(&fe), fns(f.begin(), f.end()), coefs(c.begin(), c.end()), comps(std::move(cmp))
+  {
+    if (comps.empty())
+      for (int d = 0; d < FE::dim; ++d)
+        comps.push_back(d);
+    for (int d: comps)
+      if (d < 0 || d >= FE::dim)
+        throw Error(PXG_ERR_INVALID_ARG, "AssemblyRhsAnalytic: component out of range");
+  }
 };
 
+// AssemblyS2SProjection / AssemblyProjection(c, field, feSpace, comps)
+// (include/assembly_rhs.hpp:93-163).  On a vector space the field holds every
+// component (BLOCK ordering), and the j-th listed component (default: all) is projected
+// into block j, as the reference's running block index does.
 template <typename FE>
 struct AssemblyProjection
 {
   double coef;
   std::vector<double> const * field;
   FE const * feSpace;
-  AssemblyProjection(double c, std::vector<double> const & r, FE const & fe): coef(c), field(&r), feSpace(&fe) {}
+  std::vector<int> comps;
+  AssemblyProjection(double c, std::vector<double> const & r, FE const & fe, std::vector<int> cmp = {}):
+      coef(c), field(&r), feSpace(&fe), comps(std::move(cmp))
+  {
+    if (comps.empty())
+      for (int d = 0; d < FE::dim; ++d)
+        comps.push_back(d);
+    for (int d: comps)
+      if (d < 0 || d >= FE::dim)
+        throw Error(PXG_ERR_INVALID_ARG, "AssemblyProjection: component out of range");
+    if ((int64_t)r.size() != FE::dim * fe.dof.size)
+      throw Error(PXG_ERR_INVALID_ARG, "AssemblyProjection: the field must hold every component");
+  }
 };
 
 template <typename FE>
@@ -592,6 +630,16 @@ struct Builder<void, Storage>
     calls.push_back(std::move(c));
   }
 
+  // buildRhs (builder.hpp:279-364) on one space of the system, scalar or vector: the
+  // loads are recorded and added to b by closeMatrix.  Block c of a vector space's
+  // load is condensed with the DOFs constrained in component c.
+  template <typename... Asm>
+  void buildRhs(std::tuple<Asm...> const & assemblies, std::vector<BCEss> const & bcs = {})
+  {
+    static_assert(sizeof...(Asm) > 0, "we need at least 1 assembly.");
+    std::apply([&](auto const &... a) { (addRhsCall(a, bcs), ...); }, assemblies);
+  }
+
   // setFromTriplets + prune(1., 1e-16) (builder.hpp:366-371) over the recorded calls
   void closeMatrix()
   {
@@ -649,6 +697,41 @@ struct Builder<void, Storage>
                              vals.p, bd.p, PXG_ACCUMULATE, nullptr),
             c0, "pxg_sys_assemble");
     }
+    for (auto const & r: rhsCalls)
+    {
+      Space const & sp = spaces[r.space];
+      for (auto const & part: r.parts)
+      {
+        // the constrained DOFs of component part.block, as the space's own DOF ids
+        std::vector<uint32_t> d;
+        std::vector<double> v;
+        double diag = 1.0;
+        int64_t const lo = part.block * sp.ndof;
+        for (auto const & bc: r.bcs)
+        {
+          for (size_t k = 0; k < bc.dofs.size(); ++k)
+            if ((int64_t)bc.dofs[k] >= lo && (int64_t)bc.dofs[k] < lo + sp.ndof)
+            {
+              d.push_back((uint32_t)(bc.dofs[k] - lo));
+              v.push_back(bc.values[k]);
+            }
+          diag = bc.diag;
+        }
+        check(pxg_set_bc(sp.ctx, d.data(), v.data(), (int64_t)d.size(), diag, PXG_MEM_HOST), sp.ctx, "pxg_set_bc");
+        DeviceArray<double> f;
+        if (part.field)
+          f = DeviceArray<double>(sp.ctx, (size_t)sp.ndof);
+        if (part.field)
+          check(pxg_memcpy(sp.ctx, f.p, part.field + part.fieldComp * sp.ndof, (size_t)sp.ndof * sizeof(double), 0,
+                           nullptr),
+                sp.ctx, "pxg_memcpy");
+        pxg_rhs_op op{part.kind, part.fn, part.coef, f.p, r.bcs.empty() ? 0 : 1};
+        check(pxg_assemble(sp.ctx, nullptr, nullptr, nullptr, nullptr, &op, bd.p + sp.offset + lo, PXG_ACCUMULATE,
+                           nullptr),
+              sp.ctx, "pxg_assemble");
+        // f is released here; freeing device memory waits for the assembly that reads it
+      }
+    }
     int32_t const * rp = nullptr;
     int32_t const * ci = nullptr;
     check(pxg_sys_pattern_device(S, &rp, &ci), c0, "pxg_sys_pattern_device");
@@ -665,6 +748,7 @@ struct Builder<void, Storage>
     A.values.resize((size_t)kept);
     b = bd.host();
     calls.clear(); // the triplets were consumed (builder.hpp:370)
+    rhsCalls.clear();
   }
 
 private:
@@ -681,8 +765,48 @@ private:
     std::vector<double> coefs;
     std::vector<BCEss> bcRow, bcCol;
   };
+  struct RhsPart
+  {
+    int block, kind, fn;
+    double coef;
+    double const * field; // projection: the whole field on the host, else null
+    int fieldComp;
+  };
+  struct RhsCall
+  {
+    int space;
+    std::vector<RhsPart> parts;
+    std::vector<BCEss> bcs;
+  };
   std::vector<Space> spaces;
   std::vector<Call> calls;
+  std::vector<RhsCall> rhsCalls;
+
+  template <typename FE>
+  static void checkRule()
+  {
+    // the element kernels integrate loads with the element's own rule
+    if (FE::qrType != FE::elemType)
+      throw Error(PXG_ERR_UNSUPPORTED, "buildRhs on a space with another quadrature rule");
+  }
+  template <typename X>
+  void addRhsCall(AssemblyRhsAnalytic<X> const & a, std::vector<BCEss> const & bcs)
+  {
+    checkRule<X>();
+    RhsCall r{spaceOf(*a.feSpace), {}, bcs};
+    for (int c: a.comps)
+      r.parts.push_back(RhsPart{c, 1, a.fns[(size_t)c], a.coefs[(size_t)c], nullptr, 0});
+    rhsCalls.push_back(std::move(r));
+  }
+  template <typename X>
+  void addRhsCall(AssemblyProjection<X> const & a, std::vector<BCEss> const & bcs)
+  {
+    checkRule<X>();
+    RhsCall r{spaceOf(*a.feSpace), {}, bcs};
+    for (size_t j = 0; j < a.comps.size(); ++j)
+      r.parts.push_back(RhsPart{(int)j, 2, 0, a.coef, a.field->data(), a.comps[j]});
+    rhsCalls.push_back(std::move(r));
+  }
 
   template <typename FE>
   int spaceOf(FE const & fe)

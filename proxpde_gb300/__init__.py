@@ -196,6 +196,21 @@ def _interp_coord(fe, d):
     return out
 
 
+def _component_bcs(fe, bcs, c):
+    """Set the constrained DOFs of component c of a vector space on its scalar context
+    (the context's DOF ids, values as given)."""
+    nd = fe.dof.size
+    dofs, vals = [np.zeros(0, np.int64)], [np.zeros(0)]
+    for b in bcs:
+        d, v = b.component_dofs()
+        d = d.astype(np.int64)
+        sel = (d >= c * nd) & (d < (c + 1) * nd)
+        dofs.append(d[sel] - c * nd)
+        vals.append(v[sel])
+    fe.ctx.set_bc(np.concatenate(dofs).astype(np.uint32), np.concatenate(vals), bcs[-1].diag if bcs else 1.0)
+    fe._bc_key = None
+
+
 HEX_FACES = [[0, 3, 2, 1], [3, 0, 4, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [4, 5, 6, 7]]
 
 
@@ -333,20 +348,54 @@ def _sys_op(a):
 
 
 class AssemblyRhsAnalytic:
-    """AssemblyRhsAnalytic(f, feSpace) with f chosen by id (include/assembly_rhs.hpp:34-91)."""
+    """AssemblyRhsAnalytic(f, feSpace, comps) with f chosen by id
+    (include/assembly_rhs.hpp:34-91).
 
-    def __init__(self, fn, fe, coef=1.0):
-        self.fe, self.rhs = fe, {"kind": 1, "fn": int(fn), "coef": float(coef)}
+    On a scalar space f is one function id.  On a vector space f is one id per
+    component (the components of the reference's vector function), coef one value or one
+    per component, and only the components listed in ``comps`` (default: all) get a
+    load: component c of the load goes to block c (assembly_rhs.hpp:66-73)."""
+
+    def __init__(self, fn, fe, coef=1.0, comps=None):
+        self.fe = fe
+        if fe.dim == 1:
+            if np.ndim(fn) != 0 or comps not in (None, [0], (0,)):
+                raise ValueError("AssemblyRhsAnalytic: a scalar space takes one function id")
+            self.rhs = {"kind": 1, "fn": int(fn), "coef": float(coef)}
+            self.parts = [(0, self.rhs)]
+            return
+        fns, coefs = np.asarray(fn).reshape(-1), np.broadcast_to(np.asarray(coef, dtype=np.float64), (fe.dim,))
+        if fns.size != fe.dim:
+            raise ValueError(f"AssemblyRhsAnalytic: a {fe.dim}-component space takes {fe.dim} function ids")
+        comps = range(fe.dim) if comps is None else comps
+        self.parts = [(int(c), {"kind": 1, "fn": int(fns[c]), "coef": float(coefs[c])}) for c in comps]
+        if any(not 0 <= c < fe.dim for c, _ in self.parts):
+            raise ValueError("AssemblyRhsAnalytic: component out of range")
 
 
 class AssemblyS2SProjection:
-    """AssemblyS2SProjection(c, field, feSpace) (include/assembly_rhs.hpp:93-163)."""
+    """AssemblyS2SProjection(c, field, feSpace, comps) (include/assembly_rhs.hpp:93-163).
 
-    def __init__(self, coef, field, fe):
+    On a vector space the field holds every component (BLOCK ordering, component d of
+    DOF k at k + d * ndof), and the j-th listed component of the field (default: all)
+    is projected into block j, as the reference's running block index does
+    (assembly_rhs.hpp:138-156)."""
+
+    def __init__(self, coef, field, fe, comps=None):
         import torch
 
         self.field = torch.as_tensor(np.ascontiguousarray(field, dtype=np.float64)).to(f"cuda:{fe.ctx.device}")
-        self.fe, self.rhs = fe, {"kind": 2, "coef": float(coef), "field": self.field}
+        nd = fe.dof.size
+        if self.field.numel() != nd * fe.dim:
+            raise ValueError(f"AssemblyS2SProjection: the field has {self.field.numel()} values, "
+                             f"the space {nd * fe.dim}")
+        self.fe = fe
+        self.rhs = {"kind": 2, "coef": float(coef), "field": self.field}
+        comps = range(fe.dim) if comps is None else comps
+        if any(not 0 <= int(c) < fe.dim for c in comps):
+            raise ValueError("AssemblyS2SProjection: component out of range")
+        self.parts = [(j, {"kind": 2, "coef": float(coef), "field": self.field[int(c) * nd:(int(c) + 1) * nd]})
+                      for j, c in enumerate(comps)]
 
 
 AssemblyProjection = AssemblyS2SProjection
@@ -419,11 +468,14 @@ class Builder:
         self.fe.ctx.assemble(op0=op, vals0=self.vals, b=self.b_dev if bcs else None, accumulate=True)
 
     def buildRhs(self, assemblies, bcs=()):
+        if any(a.fe.qr_type != a.fe.etype for a in assemblies):
+            # the element kernels integrate loads with the element's own rule
+            raise PxgError(6, "buildRhs on a space with another quadrature rule is not provided")
         if self.size is not None:
-            if any(a.fe.dim != 1 for a in assemblies):
-                raise PxgError(6, "buildRhs on a vector space is not provided")
             self._rhs.append((list(assemblies), list(bcs)))
             return
+        if self.fe.dim != 1:
+            raise PxgError(6, "a vector space needs Builder(numDOFs)")
         self.fe.apply_bcs(list(bcs))
         for a in assemblies:
             r = dict(a.rhs)
@@ -474,10 +526,20 @@ class Builder:
         for assemblies, bcs in self._rhs:
             for a in assemblies:
                 f = a.fe
-                f.apply_bcs(bcs)
-                r = dict(a.rhs)
-                r["apply_bc"] = 1 if bcs else 0
-                f.ctx.assemble(rhs=r, b=b[f.offset:f.offset + f.dof.size], accumulate=True)
+                f.pattern()  # the element kernels scatter through the space's own pattern
+                nd = f.dof.size
+                for blk, part in a.parts:
+                    # buildRhs zeroes the constrained rows of each block (C Fe,
+                    # include/builder.hpp:322-343): block blk is condensed with the DOFs
+                    # constrained in component blk
+                    if f.dim == 1:
+                        f.apply_bcs(bcs)
+                    else:
+                        _component_bcs(f, bcs, blk)
+                    r = dict(part)
+                    r["apply_bc"] = 1 if bcs else 0
+                    lo = f.offset + blk * nd
+                    f.ctx.assemble(rhs=r, b=b[lo:lo + nd], accumulate=True)
         rp, ci = S.get_pattern()
         torch.cuda.synchronize()
         A = sp.csr_matrix((vals.cpu().numpy(), ci, rp), shape=(S.ntot, S.ntot))

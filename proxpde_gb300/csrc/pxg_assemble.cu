@@ -997,11 +997,39 @@ __global__ void kInterpolate(int64_t nelem, double const * __restrict__ xyz, uin
 // prune(1., 1e-16): an entry is dropped when |v| <= 1e-16 (Eigen's isMuchSmallerThan)
 __device__ __forceinline__ bool pruned(double v) { return fabs(v) <= 1e-16; }
 
+// Streams the value array once: 16-byte loads, four per thread in flight (about 20 MB
+// over the grid, enough to keep HBM busy), evict-first because the values are not
+// reused by the count. A value array that starts 8 bytes off a 16-byte boundary has
+// its first entry counted alone, and an odd remainder its last.
 __global__ void kPruneCount(double const * __restrict__ vals, int64_t n, unsigned long long * out)
 {
   unsigned long long cnt = 0;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    cnt += pruned(vals[k]) ? 1ull : 0ull;
+  int64_t const head = (n > 0 && (reinterpret_cast<uintptr_t>(vals) & 15) != 0) ? 1 : 0;
+  int64_t const n2 = (n - head) / 2;
+  int64_t const t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t const stride = (int64_t)gridDim.x * blockDim.x;
+  if (t == 0)
+  {
+    if (head)
+      cnt += pruned(vals[0]) ? 1ull : 0ull;
+    if ((n - head) & 1)
+      cnt += pruned(vals[n - 1]) ? 1ull : 0ull;
+  }
+  double2 const * v2 = reinterpret_cast<double2 const *>(vals + head);
+  int64_t k = t;
+  for (; k + 3 * stride < n2; k += 4 * stride)
+  {
+    double2 const a = __ldcs(v2 + k), b = __ldcs(v2 + k + stride);
+    double2 const c = __ldcs(v2 + k + 2 * stride), d = __ldcs(v2 + k + 3 * stride);
+    cnt += (pruned(a.x) ? 1ull : 0ull) + (pruned(a.y) ? 1ull : 0ull) + (pruned(b.x) ? 1ull : 0ull) +
+           (pruned(b.y) ? 1ull : 0ull) + (pruned(c.x) ? 1ull : 0ull) + (pruned(c.y) ? 1ull : 0ull) +
+           (pruned(d.x) ? 1ull : 0ull) + (pruned(d.y) ? 1ull : 0ull);
+  }
+  for (; k < n2; k += stride)
+  {
+    double2 const a = __ldcs(v2 + k);
+    cnt += (pruned(a.x) ? 1ull : 0ull) + (pruned(a.y) ? 1ull : 0ull);
+  }
   using WR = cub::WarpReduce<unsigned long long>;
   __shared__ typename WR::TempStorage ts[8];
   unsigned long long const s = WR(ts[threadIdx.x / 32]).Sum(cnt);

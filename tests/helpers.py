@@ -167,3 +167,41 @@ def q1_quadrature(xyz, conn, k=None, chunk=131072):
             kvol += (k[e0:e0 + chunk] * ve).sum()
         rhs += (det * fq).sum()
     return vol, kvol, rhs
+
+
+def vector_load_field(n):
+    """The projected vector field of the vector-load case (the C++ test writes the same)."""
+    k = np.arange(n, dtype=np.float64)
+    return np.sin(0.37 * k) + 0.1 * (np.arange(n) % 7)
+
+
+def vector_load_expect(elem, xyz, conn, field):
+    """Expected b of the vector-load case, block by block from the oracle's scalar loads.
+
+    The case: on the unit cube, a 3-component P2 / Q2 space and a P1 / Q1 space behind
+    it (offset 3 * ndof); BCEss on the bottom (y = 0, every component) and on the left
+    (x = 0, components 0 and 2); buildRhs of AssemblyRhsAnalytic with functions (sin3,
+    const, poisson_rhs) and coefficients (1, 2, -0.5) on components 0 and 2, plus
+    AssemblyS2SProjection(0.7, field) of field components (2, 0) into blocks (0, 1);
+    and buildRhs of AssemblyRhsAnalytic(const, 3) on the scalar space without BCs.
+    Returns (b, masks of the three blocks)."""
+    tv = O.Q2HEX if elem == "hex" else O.P2TET
+    tp = O.Q1HEX if elem == "hex" else O.P1TET
+    em, nd = O.dofmap(tv, xyz.shape[0], conn)
+    emp, ndp = O.dofmap(tp, xyz.shape[0], conn)
+    dx = O.dof_coords(tv, xyz, conn, em, nd)
+    on_y0, on_x0 = O.plane_bc_mask(dx, [("y", 0.0)]), O.plane_bc_mask(dx, [("x", 0.0)])
+    masks = [on_y0 | on_x0, on_y0, on_y0 | on_x0]
+    zero = np.zeros(nd)
+
+    def load(c, rhs):
+        return O.build(tv, xyz, conn, em, nd, rhs=dict(rhs, apply_bc=1), bc_mask=masks[c], bc_val=zero)[1]
+
+    fc = [field[c * nd:(c + 1) * nd] for c in range(3)]
+    blocks = [
+        load(0, {"kind": 1, "fn": O.FN_SIN3, "c": 1.0}) + load(0, {"kind": 2, "c": 0.7, "field": fc[2]}),
+        load(1, {"kind": 2, "c": 0.7, "field": fc[0]}),
+        load(2, {"kind": 1, "fn": O.FN_POISSON_RHS, "c": -0.5}),
+        O.build(tp, xyz, conn, emp, ndp, rhs={"kind": 1, "fn": O.FN_CONST, "c": 3.0})[1],
+    ]
+    return np.concatenate(blocks), masks

@@ -12,9 +12,10 @@ SRC = os.path.join(ROOT, "tests", "cpp", "poisson3d.cpp")
 
 
 STOKES = os.path.join(ROOT, "tests", "cpp", "stokes3d.cpp")
+LOADS = os.path.join(ROOT, "tests", "cpp", "vector_loads.cpp")
 
 
-@pytest.mark.parametrize("src", [SRC, STOKES], ids=["poisson3d", "stokes3d"])
+@pytest.mark.parametrize("src", [SRC, STOKES, LOADS], ids=["poisson3d", "stokes3d", "vector_loads"])
 def test_shim_compiles(tmp_path, src):
     r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
                         src], capture_output=True, text=True)
@@ -90,3 +91,30 @@ def test_shim_stokes_goldens(engine, tmp_path, elem, expected):
     err.append(np.linalg.norm(u[3 * ndu:] - ex[3 * ndu:]))
     for e, r_ in zip(err, expected):
         assert abs(e - r_) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("elem", ["hex", "tet"])
+def test_shim_vector_loads(engine, tmp_path, elem):
+    """buildRhs on a vector space through the shim's Builder{numDOFs} (per-component
+    device functions, projection of reordered field components, component-wise BCEss)
+    against the oracle's loads block by block (tests/helpers.py:vector_load_expect)."""
+    from helpers import assert_close, vector_load_expect, vector_load_field
+    from proxpde_gb300 import Hexahedron, Tetrahedron, build, buildHyperCube
+
+    lib = build.build()
+    exe = tmp_path / "vector_loads"
+    r = subprocess.run(["g++", "-std=c++20", "-O2", "-I", os.path.join(ROOT, "include"), LOADS, "-o", str(exe),
+                        f"-L{os.path.dirname(lib)}", "-lpxg", f"-Wl,-rpath,{os.path.dirname(lib)}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), elem, str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = out.read_bytes()
+    ntot, ndu, ndp = np.frombuffer(raw[:24], dtype=np.int64)
+    b = np.frombuffer(raw, np.float64, ntot, 24)
+    assert ntot == 3 * ndu + ndp
+    mesh = buildHyperCube(Hexahedron if elem == "hex" else Tetrahedron, 3)
+    expect, _ = vector_load_expect(elem, mesh.xyz, mesh.conn, vector_load_field(3 * ndu))
+    assert_close(b, expect, what="shim vector and scalar loads")

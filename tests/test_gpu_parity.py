@@ -72,6 +72,18 @@ def test_prune_cancellation_margin(engine):
     g["ctx"].prune_count_device(v, out[1:])
     assert g["ctx"].prune_count(v) == out[1].item() == nz - g["mats"][0][1].size
     assert out[0].item() == -1
+    # the count's vector loads: a value array 8 bytes off a 16-byte boundary (first
+    # entry alone, no odd tail) and the aligned one (odd tail), with zeroed ends
+    assert nz % 2 == 1
+    npruned = nz - g["mats"][0][1].size
+    w = torch.zeros(nz + 2, dtype=torch.float64, device="cuda")  # zero sentinels count if read
+    w[1:nz + 1] = v
+    assert g["ctx"].prune_count(w[1:]) == npruned
+    extra = int(abs(g["struct_vals"][0][0]) > 1e-16) + int(abs(g["struct_vals"][0][-1]) > 1e-16)
+    w[1] = 0.0
+    w[nz] = 0.0
+    assert g["ctx"].prune_count(w[1:]) == npruned + extra
+    assert g["ctx"].prune_count(w[1:nz + 1].clone()) == npruned + extra
 
 
 @pytest.mark.parametrize("t,gen", [(O.P1TET, "tet6"), (O.P2TET, "tet5"), (O.Q1HEX, "hex"), (O.Q2HEX, "hex")])

@@ -115,3 +115,44 @@ def test_system_rejects_mismatched_operators(engine):
         S.assemble(0, 1, [(OP_TENSOR_STIFFNESS, 1.0)], vals)  # a square operator on a coupling call
     with pytest.raises(PxgError):
         S.assemble(1, 0, [(OP_GRAD, 1.0)], vals)  # grad needs vector rows
+
+
+@pytest.mark.parametrize("elem", ["hex", "tet"])
+def test_vector_loads_match_oracle(engine, elem):
+    """buildRhs on a vector space through Builder{numDOFs}: an analytic load with one
+    function per component on two of the three components, and the L2 projection of a
+    vector field with its components listed out of order, under component-wise Dirichlet
+    sets; a scalar load on the second space (tests/helpers.py:vector_load_expect). Each
+    block is compared with the oracle's scalar load of that component, condensed with
+    that component's constrained DOFs."""
+    import proxpde_gb300 as px
+    from helpers import vector_load_expect, vector_load_field
+
+    E = px.Hexahedron if elem == "hex" else px.Tetrahedron
+    mesh = px.buildHyperCube(E, 3)
+    vel = px.FESpace(mesh, 2, dim=3)
+    p = px.FESpace(mesh, 1, offset=3 * vel.dof.size)
+    nd, ndp = vel.dof.size, p.dof.size
+    field = vector_load_field(3 * nd)
+    expect, masks = vector_load_expect(elem, mesh.xyz, mesh.conn, field)
+    assert expect.size == 3 * nd + ndp
+    s = px.side
+    bcs = [px.BCEss(vel, s.BOTTOM, lambda X: np.ones((X.shape[0], 3))), px.BCEss(vel, s.LEFT, 0.0, comps=[0, 2])]
+    builder = px.Builder(3 * nd + ndp)
+    builder.buildLhs((px.AssemblyMass(1.0, vel),))
+    builder.buildRhs((px.AssemblyRhsAnalytic([px.FN_SIN3, px.FN_CONST, px.FN_POISSON_RHS], vel,
+                                             coef=[1.0, 2.0, -0.5], comps=[0, 2]),
+                      px.AssemblyS2SProjection(0.7, field, vel, comps=[2, 0])), bcs)
+    builder.buildRhs((px.AssemblyRhsAnalytic(px.FN_CONST, p, 3.0),))
+    builder.closeMatrix()
+    b = builder.b
+    for c in range(3):
+        assert masks[c].any() and np.all(b[c * nd:(c + 1) * nd][masks[c] == 1] == 0.0)
+    assert_close(b, expect, what="vector and scalar loads")
+    with pytest.raises(ValueError):
+        px.AssemblyRhsAnalytic(px.FN_CONST, vel)  # a vector space takes one id per component
+    with pytest.raises(ValueError):
+        px.AssemblyS2SProjection(1.0, field[:nd], vel)  # the field holds every component
+    pq = px.FESpace(mesh, 1, offset=0, qr_order=2)
+    with pytest.raises(px.PxgError):
+        px.Builder(ndp).buildRhs((px.AssemblyRhsAnalytic(px.FN_CONST, pq),))  # loads use the element's rule

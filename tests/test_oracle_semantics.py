@@ -120,3 +120,28 @@ def test_q1_quadrature_helper_matches_oracle():
         u = X[:, d] - 0.5
         assert abs(u @ (Ks @ u) - kvol) <= 1e-12 * kvol
     assert abs(b.sum() - rsum) <= 1e-13 * rsum
+
+
+@pytest.mark.parametrize("elem", ["hex", "tet"])
+def test_vector_load_expectation(oracle_lib, elem):
+    """The oracle side of the vector-load case (buildRhs on a vector space): blocks
+    condensed per component, the unconstrained constant load integrates to c * |cube|,
+    and block 1 holds only the projection of field component 0."""
+    from helpers import vector_load_expect, vector_load_field
+
+    xyz, conn = O.cube_hex(3) if elem == "hex" else O.cube_tet5(3)
+    tv = O.Q2HEX if elem == "hex" else O.P2TET
+    nd = O.dofmap(tv, xyz.shape[0], conn)[1]
+    field = vector_load_field(3 * nd)
+    b, masks = vector_load_expect(elem, xyz, conn, field)
+    for c in range(3):
+        blk = b[c * nd:(c + 1) * nd]
+        assert masks[c].any() and np.all(blk[masks[c] == 1] == 0.0) and np.any(blk != 0.0)
+    assert masks[1].sum() < masks[0].sum() == masks[2].sum()
+    assert abs(b[3 * nd:].sum() - 3.0) < 1e-12
+    # projection is linear in the field: doubling component 0 doubles block 1 only
+    f2 = field.copy()
+    f2[:nd] *= 2.0
+    b2, _ = vector_load_expect(elem, xyz, conn, f2)
+    assert np.allclose(b2[nd:2 * nd], 2.0 * b[nd:2 * nd], rtol=1e-14, atol=1e-300)
+    assert np.array_equal(np.delete(b2, np.s_[nd:2 * nd]), np.delete(b, np.s_[nd:2 * nd]))
