@@ -43,16 +43,21 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_element():
-    """DRAM bytes per element of the assembly kernel from the committed ncu summary."""
+def profile_figure(key):
+    """A per-element figure of the assembly kernel from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "kAssembleQ1Group_q1hex96.md")
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_element:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def traffic_per_element():
+    """DRAM bytes per element of the assembly kernel (ncu)."""
+    return profile_figure("traffic_bytes_per_element")
 
 
 def make_inputs(n, seed=20261205):
@@ -509,6 +514,19 @@ def main():
             "traffic": tpe * E if tpe else None, "traffic_source": "ncu 96^3 capture scaled by elements",
             "peak_source": which, "kernel": "kAssembleQ1Group (+memset of K, M, b)",
             "kernel_ms": asm_ms, "algorithmic_bytes": alg}
+    # the bound the kernel actually meets: instruction issue (one warp instruction per
+    # cycle per scheduler, four schedulers per SM) at the SM clock sampled during the
+    # timed region; the instruction count per element is ncu's (96^3 capture), and the
+    # time includes the memsets, so the fraction is a lower bound
+    ipe = profile_figure("warp_instructions_per_element")
+    props = torch.cuda.get_device_properties(dev)
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if ipe and mhz:
+        peak_issue = props.multi_processor_count * 4 * mhz * 1e6
+        got = E * ipe / (asm_ms * 1e-3)
+        roof["issue"] = {"warp_instructions_per_element": ipe, "achieved": got, "peak": peak_issue,
+                         "unit": "warp instructions/s", "frac": got / peak_issue,
+                         "peak_source": f"{props.multi_processor_count} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)"}
 
     e2e = None
     if not args.no_e2e:

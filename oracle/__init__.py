@@ -3,8 +3,9 @@
 This package wraps ``oracle/oracle.cpp`` (a plain C++ restatement of proxpde's
 ``Builder::buildLhs/buildRhs/closeMatrix`` element loop, see the header of that file
 for the file:line of every restated piece) with ctypes.  Only ``tests/``,
-``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` use it, as the
-checker.  The GPU engine in ``proxpde_gb300`` never imports it.
+``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` use it, to check
+results and to time the CPU baseline.  The GPU engine in ``proxpde_gb300`` never
+imports it.
 
 The helpers ``poisson_*`` re-run the reference's own golden tests on the oracle:
 build mesh -> DOF map -> BCs -> assemble -> direct solve -> ||u - I_h u||_2.

@@ -367,10 +367,10 @@ class AssemblyRhsAnalytic:
         fns, coefs = np.asarray(fn).reshape(-1), np.broadcast_to(np.asarray(coef, dtype=np.float64), (fe.dim,))
         if fns.size != fe.dim:
             raise ValueError(f"AssemblyRhsAnalytic: a {fe.dim}-component space takes {fe.dim} function ids")
-        comps = range(fe.dim) if comps is None else comps
-        self.parts = [(int(c), {"kind": 1, "fn": int(fns[c]), "coef": float(coefs[c])}) for c in comps]
-        if any(not 0 <= c < fe.dim for c, _ in self.parts):
+        comps = list(range(fe.dim)) if comps is None else [int(c) for c in comps]
+        if any(not 0 <= c < fe.dim for c in comps):
             raise ValueError("AssemblyRhsAnalytic: component out of range")
+        self.parts = [(c, {"kind": 1, "fn": int(fns[c]), "coef": float(coefs[c])}) for c in comps]
 
 
 class AssemblyS2SProjection:

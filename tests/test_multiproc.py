@@ -1,7 +1,7 @@
 """The multi-rank host logic of bench.py on CPU with gloo (world size 2): the job time
 is the maximum over the ranks, and the reference arm under torchrun prints one line
-from rank 0 while the other rank exits cleanly.  (Every GPU machine of this build has one
-GPU, so the N > 1 GPU path is replicas of this logic.)"""
+from rank 0 while the other rank exits cleanly.  (With more than one GPU, bench.py
+runs one replica of the workload per rank under this same logic.)"""
 import json
 import os
 import socket
