@@ -226,9 +226,10 @@ struct FESpace
   } dof;
   int64_t nnz = 0;
   int64_t offset = 0;
+  int64_t nelem = 0;
   double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.}; // bounding box of the mesh
 
-  explicit FESpace(Mesh<Elem> const & m, int64_t off = 0, int device = 0): offset(off)
+  explicit FESpace(Mesh<Elem> const & m, int64_t off = 0, int device = 0): offset(off), nelem(m.nelem())
   {
     check(pxg_create(&ctx, device), nullptr, "pxg_create");
     check(pxg_set_mesh(ctx, elemType, m.xyz.data(), m.nnodes(), m.conn.data(), m.nelem(), PXG_MEM_HOST), ctx,
@@ -356,6 +357,17 @@ struct AssemblyScalarMass
 template <typename FE>
 using AssemblyMass = AssemblyScalarMass<FE>;
 
+// AssemblyMassFE with a P0 coefficient: one value per element (the space holds one
+// per-element coefficient: with AssemblyStiffnessFE in the same call, both take the
+// same values)
+template <typename FE>
+struct AssemblyMassFE
+{
+  std::vector<double> const * coefP0;
+  FE const * feSpace;
+  AssemblyMassFE(std::vector<double> const & k, FE const & fe): coefP0(&k), feSpace(&fe) {}
+};
+
 // AssemblyRhsAnalytic(f, feSpace, comps) (include/assembly_rhs.hpp:34-91) with device
 // functions chosen by id.  A scalar space takes one id; a vector space takes one id
 // and one coefficient per component (the components of the reference's vector
@@ -473,6 +485,7 @@ struct Builder
   {
     static_assert(sizeof...(Asm) > 0, "we need at least 1 assembly.");
     pxg_lhs_op op{0, 0.0, 0, 0.0, bcs.empty() ? 0 : 1};
+    p0 = nullptr;
     std::apply([&](auto const &... a) { (addLhs(op, a), ...); }, assemblies);
     setBcs(bcs);
     check(pxg_assemble(fe.ctx, &op, vals.p, nullptr, nullptr, nullptr, bcs.empty() ? nullptr : bDev.p,
@@ -558,12 +571,30 @@ private:
     op.stiffness = 1;
     op.stiff_coef = a.coef;
   }
+  // the per-element coefficient of the current buildLhs call
+  std::vector<double> const * p0 = nullptr;
+  void setP0(std::vector<double> const & k)
+  {
+    if (p0 && p0 != &k && *p0 != k)
+      throw Error(PXG_ERR_UNSUPPORTED, "the per-element coefficients of one buildLhs call must be the same");
+    if ((int64_t)k.size() != fe.nelem)
+      throw Error(PXG_ERR_INVALID_ARG, "a per-element coefficient needs one value per element");
+    p0 = &k;
+    check(pxg_set_coef(fe.ctx, k.data(), PXG_MEM_HOST, nullptr), fe.ctx, "pxg_set_coef");
+  }
   template <typename X>
   void addLhs(pxg_lhs_op & op, AssemblyStiffnessFE<X> const & a)
   {
-    check(pxg_set_coef(fe.ctx, a.coefP0->data(), PXG_MEM_HOST, nullptr), fe.ctx, "pxg_set_coef");
+    setP0(*a.coefP0);
     op.stiffness = 2;
     op.stiff_coef = 1.0;
+  }
+  template <typename X>
+  void addLhs(pxg_lhs_op & op, AssemblyMassFE<X> const & a)
+  {
+    setP0(*a.coefP0);
+    op.mass = 2;
+    op.mass_coef = 1.0;
   }
   template <typename X>
   void addLhs(pxg_lhs_op & op, AssemblyScalarMass<X> const & a)

@@ -82,6 +82,8 @@ typedef struct pxg_ctx pxg_ctx;
  *             2: AssemblyStiffnessFE with the per-element (P0 FEVar) coefficient set by
  *                pxg_set_coef, times stiff_coef         (include/assembly_lhs.hpp:77-113)
  *   mass      0: none, 1: AssemblyScalarMass(mass_coef) (include/assembly_lhs.hpp:191-231)
+ *             2: AssemblyMassFE with the per-element coefficient set by pxg_set_coef,
+ *                times mass_coef                        (include/assembly_lhs.hpp:234-277)
  *   apply_bc  condense with the context's essential BCs (include/builder.hpp:76-124);
  *             the lifted load C(-Ke h) and h at constrained DOFs go into b as the
  *             reference's buildLhs does (builder.hpp:102, 119, 137). */

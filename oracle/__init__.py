@@ -36,6 +36,7 @@ class OrcLhs(C.Structure):
         ("mass_kind", C.c_int32),
         ("mass_c", C.c_double),
         ("apply_bc", C.c_int32),
+        ("m_e", C.POINTER(C.c_double)),
     ]
 
 
@@ -178,12 +179,15 @@ def interpolate(t, xyz, conn, em, ndof, fn, c=1.0):
 def _lhs(lhs, keep):
     if lhs is None:
         return None
-    k_e = lhs.get("k_e")
+    k_e, m_e = lhs.get("k_e"), lhs.get("m_e")
     if k_e is not None:
         k_e = np.ascontiguousarray(k_e, dtype=np.float64)
         keep.append(k_e)
+    if m_e is not None:
+        m_e = np.ascontiguousarray(m_e, dtype=np.float64)
+        keep.append(m_e)
     s = OrcLhs(int(lhs.get("stiff_kind", 0)), float(lhs.get("stiff_c", 0.0)), _dp(k_e),
-               int(lhs.get("mass_kind", 0)), float(lhs.get("mass_c", 0.0)), int(lhs.get("apply_bc", 0)))
+               int(lhs.get("mass_kind", 0)), float(lhs.get("mass_c", 0.0)), int(lhs.get("apply_bc", 0)), _dp(m_e))
     return C.pointer(s)
 
 

@@ -377,9 +377,10 @@ struct orc_lhs
   int32_t stiff_kind;  // 0 none, 1 constant coefficient, 2 per-element coefficient (P0 FEVar)
   double stiff_c;      // the constant (kind 1)
   double const * k_e;  // per-element values (kind 2)
-  int32_t mass_kind;   // 0 none, 1 constant coefficient
-  double mass_c;
+  int32_t mass_kind;   // 0 none, 1 constant coefficient, 2 per-element coefficient (P0 FEVar)
+  double mass_c;       // the constant (kind 1)
   int32_t apply_bc;    // condense with the essential BC set (builder.hpp:76-124)
+  double const * m_e;  // per-element values (mass kind 2)
 };
 
 struct orc_rhs
@@ -628,10 +629,12 @@ int orc_element(int t, double const * xyz, uint32_t const * conn, int64_t e,
     }
     if (lhs && lhs->mass_kind)
     {
-      // AssemblyScalarMass (assembly_lhs.hpp:207-221)
+      // AssemblyScalarMass (assembly_lhs.hpp:207-221) / AssemblyMassFE with a P0
+      // coefficient (:262-277: coef = 1, FEVar::evaluate = 1 * m_e)
+      double const c = lhs->mass_kind == 1 ? lhs->mass_c : 1.0 * lhs->m_e[e];
       for (int q = 0; q < nq; ++q)
       {
-        double const s = lhs->mass_c * fe->JxW[q];
+        double const s = c * fe->JxW[q];
         double const * p = &fe->phiRef[q * N];
         for (int i = 0; i < N; ++i)
         {

@@ -300,7 +300,8 @@ class AssemblyStiffnessFE:
     (include/assembly_lhs.hpp:77-113)."""
 
     def __init__(self, k_e, fe, scale=1.0):
-        fe.set_coefficient(k_e)
+        self.k_e = np.ascontiguousarray(k_e, dtype=np.float64)
+        fe.set_coefficient(self.k_e)
         self.fe, self.op = fe, {"stiffness": 2, "stiff_coef": float(scale)}
 
 
@@ -312,6 +313,17 @@ class AssemblyScalarMass:
 
 
 AssemblyMass = AssemblyScalarMass
+
+
+class AssemblyMassFE:
+    """AssemblyMassFE(coefP0, feSpace) with a per-element (P0) coefficient
+    (include/assembly_lhs.hpp:234-277).  The space holds one per-element coefficient:
+    with AssemblyStiffnessFE in the same call, both must be given the same values."""
+
+    def __init__(self, k_e, fe, scale=1.0):
+        self.k_e = np.ascontiguousarray(k_e, dtype=np.float64)
+        fe.set_coefficient(self.k_e)
+        self.fe, self.op = fe, {"mass": 2, "mass_coef": float(scale)}
 
 
 class AssemblyTensorStiffness:
@@ -452,6 +464,13 @@ class Builder:
         op = {"stiffness": 0, "stiff_coef": 0.0, "mass": 0, "mass_coef": 0.0, "apply_bc": 1 if bcs else 0}
         if len(assemblies) == 0:
             raise ValueError("we need at least 1 assembly.")
+        # the space holds one per-element coefficient: the call's P0 assemblies share it,
+        # and it is set again here (another assembly may have been built since)
+        coefs = [a.k_e for a in assemblies if getattr(a, "k_e", None) is not None]
+        if any(not np.array_equal(c, coefs[0]) for c in coefs[1:]):
+            raise PxgError(6, "the per-element coefficients of one buildLhs call must be the same")
+        if coefs:
+            self.fe.set_coefficient(coefs[0])
         for a in assemblies:
             o = getattr(a, "op", None)
             if o is None:

@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(NT) kAssemble(AsmArgs a)
         if (op.stiff)
           val += (op.stiff == 2 ? op.sc * kfac : op.sc) * kv;
         if (op.mass)
-          val += op.mc * mv;
+          val += massCoef(op, kfac) * mv;
         if (op.bc && cons)
         {
           bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
@@ -742,7 +742,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
   bool const k0 = op0.on && op0.stiff, k1 = op1.on && op1.stiff;
   bool const m0 = op0.on && op0.mass, m1 = op1.on && op1.mass;
   bool const needK = k0 || k1, needM = m0 || m1;
-  bool const kE = (k0 && op0.stiff == 2) || (k1 && op1.stiff == 2);
+  bool const kE = usesCoef(op0) || usesCoef(op1);
   double const kfac = (kE && a.kE) ? a.kE[e] : 1.0;
 
   // --- geometry in double-float: J columns = vertex differences
@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
   bool const foldK = k0 != k1, foldM = m0 != m1;
   double const ks0 = k0 ? (op0.stiff == 2 ? op0.sc * kfac : op0.sc) : 0.;
   double const ks1 = k1 ? (op1.stiff == 2 ? op1.sc * kfac : op1.sc) : 0.;
-  double const ms0 = m0 ? op0.mc : 0., ms1 = m1 ? op1.mc : 0.;
+  double const ms0 = m0 ? massCoef(op0, kfac) : 0., ms1 = m1 ? massCoef(op1, kfac) : 0.;
   dfl G[6];
   {
     dfl const s = fromDouble<dfl>(foldK ? (k0 ? ks0 : ks1) : 1.0) * rcp(adet);
@@ -1291,11 +1291,11 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     if (!ops[m])
       continue;
     pxg_lhs_op const & o = *ops[m];
-    if (o.stiffness < 0 || o.stiffness > 2 || o.mass < 0 || o.mass > 1)
+    if (o.stiffness < 0 || o.stiffness > 2 || o.mass < 0 || o.mass > 2)
       return fail(c, PXG_ERR_INVALID_ARG, "lhs op %d: bad stiffness/mass kind", m);
     if (!outs[m])
       return fail(c, PXG_ERR_INVALID_ARG, "lhs op %d has no output array", m);
-    if (o.stiffness == 2 && !c->hasCoef)
+    if ((o.stiffness == 2 || o.mass == 2) && !c->hasCoef)
       return fail(c, PXG_ERR_INVALID_ARG, "lhs op %d needs the per-element coefficient (pxg_set_coef)", m);
     a.op[m] = LhsDev{1, o.stiffness, o.mass, o.apply_bc, o.stiff_coef, o.mass_coef, outs[m]};
     any = true;

@@ -342,6 +342,19 @@ struct LhsDev
   double * vals;
 };
 
+// The mass coefficient of an operator for an element whose P0 coefficient is kfac:
+// AssemblyScalarMass(mc) (kind 1) or AssemblyMassFE with the per-element coefficient
+// (kind 2, include/assembly_lhs.hpp:234-277), times mc.
+__host__ __device__ __forceinline__ double massCoef(LhsDev const & op, double kfac)
+{
+  return op.mass == 2 ? op.mc * kfac : op.mc;
+}
+// whether an operator reads the per-element coefficient
+__host__ __device__ __forceinline__ bool usesCoef(LhsDev const & op)
+{
+  return op.on && (op.stiff == 2 || op.mass == 2);
+}
+
 struct AsmArgs
 {
   int64_t nelem;

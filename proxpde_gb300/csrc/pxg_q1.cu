@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(128) kAssembleQ1(AsmArgs a)
     if (!op.on)
       continue;
     T const ks = fromDouble<T>(op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.);
-    T const ms = fromDouble<T>(op.mass ? op.mc : 0.);
+    T const ms = fromDouble<T>(op.mass ? massCoef(op, kfac) : 0.);
     constexpr int IU = kFull<T>(8);
 #pragma unroll IU
     for (int i = 0; i < 8; ++i)
@@ -845,7 +845,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   {
     sw[kSwCons] = cons;
     // the element's coefficient for phase C, in the slot's spare ninth word of bv
-    bool const needKE = (a.op[0].on && a.op[0].stiff == 2) || (a.op[1].on && a.op[1].stiff == 2);
+    bool const needKE = usesCoef(a.op[0]) || usesCoef(a.op[1]);
     bv[8] = (needKE && a.kE) ? a.kE[e] : 1.0;
   }
   if (lhs)
@@ -1093,7 +1093,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) kAssembleQ1Group(AsmArgs a)
   {
     LhsDev const & op = a.op[m];
     ks[m] = fromDouble<T>(op.stiff ? (op.stiff == 2 ? op.sc * kfac : op.sc) : 0.);
-    ms[m] = fromDouble<T>(op.mass ? op.mc : 0.);
+    ms[m] = fromDouble<T>(op.mass ? massCoef(op, kfac) : 0.);
   }
   uint32_t const * const ss = slotw + s * kSlotWords;
   double const * const bs = bvAll + s * kBvStride;

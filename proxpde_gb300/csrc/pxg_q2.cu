@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(NT) kAssembleQ2(AsmArgs a)
   bool const k0 = op0.on && op0.stiff, k1 = op1.on && op1.stiff;
   bool const m0 = op0.on && op0.mass, m1 = op1.on && op1.mass;
   bool const needK = k0 || k1, needM = m0 || m1;
-  bool const kE = (k0 && op0.stiff == 2) || (k1 && op1.stiff == 2);
+  bool const kE = usesCoef(op0) || usesCoef(op1);
   bool const foldK = k0 != k1, foldM = m0 != m1;
   bool const anyBcOp = (op0.on && op0.bc) || (op1.on && op1.bc);
   bool const lhs = op0.on || op1.on;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(NT) kAssembleQ2(AsmArgs a)
       double const ksF = foldK ? (k0 ? (op0.stiff == 2 ? op0.sc * kfac : op0.sc)
                                      : (op1.stiff == 2 ? op1.sc * kfac : op1.sc))
                                : 1.0;
-      double const msF = foldM ? (m0 ? op0.mc : op1.mc) : 1.0;
+      double const msF = foldM ? massCoef(m0 ? op0 : op1, kfac) : 1.0;
       dfl const s = (toDfl(ksF) * wq) * rcp(adet);
       st(sG + 6 * t + 0, s * dot3(A[0][0], A[0][0], A[0][1], A[0][1], A[0][2], A[0][2]));
       st(sG + 6 * t + 1, s * dot3(A[1][0], A[1][0], A[1][1], A[1][1], A[1][2], A[1][2]));
@@ -295,6 +295,8 @@ __global__ void __launch_bounds__(NT) kAssembleQ2(AsmArgs a)
     uint16_t const * rk = a.rank + e * (int64_t)(N * N);
     double const kd0 = k0 ? (op0.stiff == 2 ? op0.sc * ((kE && a.kE) ? a.kE[e] : 1.0) : op0.sc) : 0.;
     double const kd1 = k1 ? (op1.stiff == 2 ? op1.sc * ((kE && a.kE) ? a.kE[e] : 1.0) : op1.sc) : 0.;
+    double const md0 = m0 ? massCoef(op0, (kE && a.kE) ? a.kE[e] : 1.0) : 0.;
+    double const md1 = m1 ? massCoef(op1, (kE && a.kE) ? a.kE[e] : 1.0) : 0.;
     for (int p = t; p < NP; p += NT)
     {
       uint16_t const pr = gPairs[p];
@@ -336,10 +338,10 @@ __global__ void __launch_bounds__(NT) kAssembleQ2(AsmArgs a)
         {
           v = foldK ? kv : toDfl(m ? kd1 : kd0) * kv;
           if (op.mass)
-            v = v + (foldM ? mv : toDfl(op.mc) * mv);
+            v = v + (foldM ? mv : toDfl(m ? md1 : md0) * mv);
         }
         else
-          v = foldM ? mv : toDfl(op.mc) * mv;
+          v = foldM ? mv : toDfl(m ? md1 : md0) * mv;
         double const val = toDouble(v);
         if (op.bc && (ci || cj))
         {

@@ -68,6 +68,8 @@ def oracle_lhs(op, k):
          "mass_c": op.get("mass_coef", 1.0), "apply_bc": op.get("apply_bc", 0)}
     if d["stiff_kind"] == 2:
         d["k_e"] = np.asarray(k) * op.get("stiff_coef", 1.0)
+    if d["mass_kind"] == 2:
+        d["m_e"] = np.asarray(k) * op.get("mass_coef", 1.0)
     return d
 
 

@@ -241,6 +241,41 @@ def test_tet_kernels_agree_with_oracle(engine, monkeypatch, kernel, t, gen, n, b
     assert_close(g["b"], b, what="rhs")
 
 
+MASS_FE_KERNELS = [(O.P1TET, "tet6", 5, {}), (O.P2TET, "tet6", 3, {}), (O.P2TET, "tet6", 3, {"PXG_TET_FP64": "1"}),
+                   (O.Q1HEX, "hex", 5, {}), (O.Q1HEX, "hex", 5, {"PXG_Q1_THREAD": "1"}),
+                   (O.Q1HEX, "hex", 4, {"PXG_Q1_GENERIC": "1"}), (O.Q2HEX, "hex", 3, {}),
+                   (O.Q2HEX, "hex", 2, {"PXG_Q2_FP64": "1"})]
+
+
+@pytest.mark.parametrize("t,gen,n,env", MASS_FE_KERNELS,
+                         ids=["p1", "p2", "p2_fp64", "q1", "q1_thread", "q1_generic", "q2", "q2_fp64"])
+def test_mass_fe_coefficient_matches_oracle(engine, monkeypatch, t, gen, n, env):
+    """AssemblyMassFE with the per-element coefficient (mass kind 2, times mass_coef)
+    in every element kernel against the oracle: alone (the mass coefficient folded
+    where a kernel folds a single operator's), beside AssemblyStiffnessFE on the same
+    coefficient, and in one operator with a constant stiffness, with Dirichlet data."""
+    for v in ("PXG_TET_FP64", "PXG_Q1_THREAD", "PXG_Q1_GENERIC", "PXG_Q2_FP64"):
+        monkeypatch.setenv(v, env.get(v, "0"))
+    xyz, conn, k = problem(gen, n, 0.15, seed=29, sigma=1.0)
+    em, ndof = O.dofmap(t, xyz.shape[0], conn)
+    dx = O.dof_coords(t, xyz, conn, em, ndof)
+    mask = O.plane_bc_mask(dx, [("z", 0.0)])
+    val = np.where(mask, 1.0 - dx[:, 0], 0.0)
+    dofs = np.nonzero(mask)[0].astype(np.uint32)
+    for ops in ([{"mass": 2, "mass_coef": 0.75}],
+                [{"stiffness": 2, "stiff_coef": 1.0}, {"mass": 2, "mass_coef": 2.0}],
+                [{"stiffness": 1, "stiff_coef": 0.5, "mass": 2, "mass_coef": 3.0, "apply_bc": 1}]):
+        bc = (dofs, val[dofs]) if any(o.get("apply_bc") for o in ops) else None
+        g = gpu_assemble(t, xyz, conn, ops, k=k, bc=bc)
+        for op, mat in zip(ops, g["mats"]):
+            o = oracle_lhs(op, k)
+            kw = dict(bc_mask=mask, bc_val=val) if op.get("apply_bc") else {}
+            csr, b = O.build(t, xyz, conn, em, ndof, lhs=o, **kw)
+            compare_csr(mat, csr, ndof)
+            if op.get("apply_bc"):
+                assert_close(g["b"], b, what="lift")
+
+
 @pytest.mark.parametrize("kernel", ["dfl", "fp64"])
 def test_q1_two_stiffness_operators(engine, monkeypatch, kernel):
     """The Q1 group kernel with two stiffness operators of different coefficients, one

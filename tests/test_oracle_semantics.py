@@ -145,3 +145,22 @@ def test_vector_load_expectation(oracle_lib, elem):
     b2, _ = vector_load_expect(elem, xyz, conn, f2)
     assert np.allclose(b2[nd:2 * nd], 2.0 * b[nd:2 * nd], rtol=1e-14, atol=1e-300)
     assert np.array_equal(np.delete(b2, np.s_[nd:2 * nd]), np.delete(b, np.s_[nd:2 * nd]))
+
+
+@pytest.mark.parametrize("t,gen", [(O.P1TET, "tet6"), (O.P2TET, "tet6"), (O.Q1HEX, "hex"), (O.Q2HEX, "hex")])
+def test_mass_fe_coefficient(oracle_lib, t, gen):
+    """AssemblyMassFE with a P0 coefficient (assembly_lhs.hpp:262-277): a constant
+    coefficient reproduces AssemblyScalarMass, and the element matrix scales with the
+    element's own value only."""
+    from helpers import problem
+
+    xyz, conn, k = problem(gen, 2, 0.15, seed=3, sigma=1.0)
+    em, ndof = O.dofmap(t, xyz.shape[0], conn)
+    c = np.full(conn.shape[0], 2.5)
+    a, _ = O.build(t, xyz, conn, em, ndof, lhs={"mass_kind": 2, "m_e": c})
+    b, _ = O.build(t, xyz, conn, em, ndof, lhs={"mass_kind": 1, "mass_c": 2.5})
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    for e in (0, conn.shape[0] - 1):
+        Me, _ = O.element(t, xyz, conn, e, lhs={"mass_kind": 2, "m_e": k})
+        M1, _ = O.element(t, xyz, conn, e, lhs={"mass_kind": 1, "mass_c": 1.0})
+        assert np.allclose(Me, k[e] * M1, rtol=1e-15, atol=0.0)
