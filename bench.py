@@ -14,6 +14,11 @@ separately as `setup_s`).  Inputs are synthetic (seeded), not a dataset.
 
 Prints one JSON line.  Under torchrun (N > 1) every rank assembles its own replica
 (weak scaling) and rank 0 prints the aggregate over ranks (max time over ranks).
+Besides the contract's keys: `roofline.issue` (the instruction-issue bound the Q1
+kernel meets), `e2e.host` (the GPU's NUMA node and the CPUs the host-buffer leg ran
+on), `configs` (P1 16^3 x 6, P2 64^3 x 6, Q2 48^3), `adjoint` (Q1 96^3 gradient),
+`batched` (256 ragged problems, batched vs one at a time) and `widened` (Dirichlet
+setup from facet markers, Taylor-Hood Stokes systems).
 """
 from __future__ import annotations
 
