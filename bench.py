@@ -3,22 +3,26 @@
 
 Workload (one step): the perturbed 128^3 Q1-hex unit cube (2,097,152 elements,
 2,146,689 nodes; interior nodes moved by a seeded U(-0.2h, 0.2h) per coordinate),
-per-element diffusivity k_e = exp(N(0,1)), 2x2x2 Gauss quadrature, FP64:
-stiffness (AssemblyStiffnessFE with the P0 coefficient) and mass (AssemblyMass(1))
-CSR values plus the load vector of f = sin(pi x) sin(pi y) sin(pi z), assembled in
-one fused pass on the device-resident structural pattern, followed by closeMatrix's
-prune check of both matrices.  The mesh, DOF map and pattern are built once (timed
-separately as `setup_s`).  Inputs are synthetic (seeded), not a dataset.
+per-element diffusivity k_e = exp(N(0,1)), 2x2x2 Gauss quadrature, computed in FP64
+arithmetic (IEEE binary64, as the reference): stiffness (AssemblyStiffnessFE with the
+P0 coefficient) and mass (AssemblyMass(1)) CSR values plus the load vector of
+f = sin(pi x) sin(pi y) sin(pi z), assembled in one fused pass on the device-resident
+structural pattern, followed by closeMatrix's prune check of both matrices.  The mesh,
+DOF map and pattern are built once (timed separately as `setup_s`).  Inputs are
+synthetic (seeded), not a dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 128]
 
 Prints one JSON line.  Under torchrun (N > 1) every rank assembles its own replica
 (weak scaling) and rank 0 prints the aggregate over ranks (max time over ranks).
-Besides the contract's keys: `roofline.issue` (the instruction-issue bound the Q1
-kernel meets), `e2e.host` (the GPU's NUMA node and the CPUs the host-buffer leg ran
-on), `configs` (P1 16^3 x 6, P2 64^3 x 6, Q2 48^3), `adjoint` (Q1 96^3 gradient),
-`batched` (256 ragged problems, batched vs one at a time) and `widened` (Dirichlet
-setup from facet markers, Taylor-Hood Stokes systems).
+Besides the contract's keys: `roofline.fp64` (the FP64 pipe, the bound the FP64
+kernel meets: FP64 instructions per second against the FMA rate measured live by
+pxg_fp64_rate), `dfl` (the same workload with the opt-in double-float kernels and
+their largest entrywise deviation from the FP64 result), `e2e.host` (the GPU's NUMA
+node and the CPUs the host-buffer leg ran on), `configs` (P1 16^3 x 6, P2 64^3 x 6,
+Q2 48^3), `adjoint` (Q1 96^3 gradient), `batched` (256 ragged problems, batched vs
+one at a time) and `widened` (Dirichlet setup from facet markers, Taylor-Hood Stokes
+systems).
 """
 from __future__ import annotations
 
@@ -48,9 +52,12 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_figure(key):
+PROFILE = "kAssembleQ1F64_q1hex96.md"
+
+
+def profile_figure(key, name=PROFILE):
     """A per-element figure of the assembly kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "kAssembleQ1Group_q1hex96.md")
+    p = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(p):
             if line.startswith(key + ":"):
@@ -232,10 +239,10 @@ def measure_configs(peak_gbs, reps=5):
 
     out = {}
     cases = (("p1tet_16", L.P1TET, meshgen.cube_tet6, 16, 0.0, None, 1, {"kind": 1, "fn": L.FN_CONST, "coef": 1.0},
-              "kAssembleTet<P1>"),
-             ("p2tet_64", L.P2TET, meshgen.cube_tet6, 64, 0.15, 0.5, 2, None, "kAssembleTet<P2>"),
+              "kAssembleTet64<P1>"),
+             ("p2tet_64", L.P2TET, meshgen.cube_tet6, 64, 0.15, 0.5, 2, None, "kAssembleTet64<P2>"),
              ("q2hex_48", L.Q2HEX, meshgen.cube_hex, 48, 0.2, 1.0, 2, {"kind": 1, "fn": L.FN_SIN3, "coef": 1.0},
-              "kAssembleQ2"))
+              "kAssemble<Q2HEX>"))
     for name, t, gen, n, alpha, sigma, nmat, rhs, kern in cases:
         xyz, conn = gen(n)
         if alpha:
@@ -253,25 +260,33 @@ def measure_configs(peak_gbs, reps=5):
         M = torch.empty_like(K) if nmat == 2 else None
         b = torch.empty(ndof, dtype=torch.float64, device="cuda") if rhs else None
         kw = dict(op0=opK, vals0=K, op1={"mass": 1, "mass_coef": 1.0} if M is not None else None, vals1=M, rhs=rhs, b=b)
-        for _ in range(2):
-            ctx.assemble(**kw)
-        torch.cuda.synchronize()
-        ts = []
-        for _ in range(reps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            ctx.assemble(**kw)
-            e1.record()
+
+        def best_ms():
+            for _ in range(2):
+                ctx.assemble(**kw)
             torch.cuda.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        ms = min(ts)
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                ctx.assemble(**kw)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return min(ts)
+
+        ms = best_ms()
+        ctx.set_arithmetic(L.ARITH_DFL)
+        dms = best_ms()
         N = {L.P1TET: 4, L.P2TET: 10, L.Q1HEX: 8, L.Q2HEX: 27}[t]
         B = 4 * conn.shape[1] * E + 4 * N * E + (8 * E if sigma else 0) + 24 * xyz.shape[0] + 8 * nnz * nmat + \
             (8 * ndof if rhs else 0)
         gbs = B / (ms * 1e-3) / 1e9
         out[name] = {"elements": int(E), "ndof": int(ndof), "nnz": int(nnz), "ms": ms, "elements_per_s": E / (ms * 1e-3),
-                     "kernel": kern, "algorithmic_bytes": int(B), "achieved_gbs": gbs, "frac_hbm": gbs / peak_gbs,
-                     "includes": "memset of the outputs + element kernel"}
+                     "kernel": kern, "dtype": "f64", "algorithmic_bytes": int(B), "achieved_gbs": gbs,
+                     "frac_hbm": gbs / peak_gbs, "includes": "memset of the outputs + element kernel",
+                     "dfl_ms": dms, "dfl_kernel": {L.P1TET: "kAssembleTet<P1>", L.P2TET: "kAssembleTet<P2>",
+                                                   L.Q2HEX: "kAssembleQ2"}[t]}
         del ctx, K, M, b
         torch.cuda.empty_cache()
     return out
@@ -425,6 +440,7 @@ def main():
     ap.add_argument("--no-widened", action="store_true", help="skip the Dirichlet-setup and Stokes measurements")
     ap.add_argument("--no-configs", action="store_true", help="skip the P1 / P2 / Q2 workload measurements")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-dfl", action="store_true", help="skip the double-float comparison leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-gradient measurement")
     args = ap.parse_args()
@@ -517,21 +533,58 @@ def main():
     tpe = traffic_per_element()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": tpe * E if tpe else None, "traffic_source": "ncu 96^3 capture scaled by elements",
-            "peak_source": which, "kernel": "kAssembleQ1Group (+memset of K, M, b)",
+            "peak_source": which, "kernel": "kAssembleQ1F64 (+memset of K, M, b)",
             "kernel_ms": asm_ms, "algorithmic_bytes": alg}
-    # the bound the kernel actually meets: instruction issue (one warp instruction per
-    # cycle per scheduler, four schedulers per SM) at the SM clock sampled during the
-    # timed region; the instruction count per element is ncu's (96^3 capture), and the
-    # time includes the memsets, so the fraction is a lower bound
-    ipe = profile_figure("warp_instructions_per_element")
-    props = torch.cuda.get_device_properties(dev)
-    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
-    if ipe and mhz:
-        peak_issue = props.multi_processor_count * 4 * mhz * 1e6
-        got = E * ipe / (asm_ms * 1e-3)
-        roof["issue"] = {"warp_instructions_per_element": ipe, "achieved": got, "peak": peak_issue,
-                         "unit": "warp instructions/s", "frac": got / peak_issue,
-                         "peak_source": f"{props.multi_processor_count} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)"}
+    # the bound the FP64 kernel meets: the FP64 pipe.  FP64 instructions per element from
+    # ncu (96^3 capture: DFMA + DMUL + DADD thread instructions / elements) times the
+    # elements over the event-timed launch, against the FMA rate measured now on this
+    # GPU; the launch time includes the memsets, so the fraction is a lower bound
+    from proxpde_gb300._lib import fp64_rate
+
+    rate, rate_ms = fp64_rate(dev)
+    fpe = profile_figure("fp64_instructions_per_element")
+    roof["fp64"] = {"fp64_instructions_per_element": fpe, "peak": rate, "unit": "FP64 instructions/s",
+                    "peak_source": f"pxg_fp64_rate: independent FMA chains, event-timed ({rate_ms:.2f} ms launch)"}
+    if fpe:
+        got = E * fpe / (asm_ms * 1e-3)
+        roof["fp64"].update({"achieved": got, "frac": got / rate})
+
+    # the opt-in double-float kernel on the same workload, and its largest entrywise
+    # deviation from the FP64 result (entries above 1e-8 of the matrix's largest)
+    dfl = None
+    if not args.no_dfl:
+        from proxpde_gb300._lib import ARITH_DFL
+
+        cd = Context(dev)
+        cd.set_arithmetic(ARITH_DFL)
+        cd.set_mesh(L.Q1HEX, xyz, conn)
+        cd.build_dofmap()
+        cd.build_pattern()
+        cd.set_coef(k)
+        Kd, Md, bd = torch.empty_like(K), torch.empty_like(M), torch.empty_like(b)
+        kw = dict(op0=opK, vals0=Kd, op1=opM, vals1=Md, rhs=rhs, b=bd, stream=sp)
+        for _ in range(3):
+            cd.assemble(**kw)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            cd.assemble(**kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dms = e0.elapsed_time(e1) / args.steps
+        ctx.assemble(op0=opK, vals0=K, op1=opM, vals1=M, rhs=rhs, b=b, stream=sp)
+        torch.cuda.synchronize()
+
+        def dev_rel(x, y):
+            big = y.abs() > 1e-8 * y.abs().max()
+            return float(((x - y).abs()[big] / y.abs()[big]).max())
+
+        dfl = {"kernel": "kAssembleQ1Group<dfl> (+memset of K, M, b)", "ms": dms, "elements_per_s": E / (dms * 1e-3),
+               "arithmetic": "double-float (unevaluated f32 pairs, ~48-bit significand) on the FP32 pipes; FP64 for "
+                             "the coordinate differences, the final hi+lo sums and the reductions",
+               "max_rel_dev_from_fp64": {"K": dev_rel(Kd, K), "M": dev_rel(Md, M), "b": dev_rel(bd, b)}}
+        del cd, Kd, Md, bd
+        torch.cuda.empty_cache()
 
     e2e = None
     if not args.no_e2e:
@@ -621,15 +674,15 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32x2+f64",
-            "arithmetic": "double-float (unevaluated f32 pairs, ~48-bit significand) on the FP32 pipes; FP64 for "
-                          "the coordinate differences, the final hi+lo sums and the reductions; f64 outputs",
+            "vs_baseline": None, "dtype": "f64",
+            "arithmetic": "IEEE binary64 throughout (geometry, local matrices, sums, reductions); FP64-pipe bound",
             "data": "synthetic (seeded perturbed cube)",
             "config": {"workload": f"q1hex perturbed {n}^3: K(k_e)+M+rhs sin3, fused pass + prune check",
                        "elements": E, "nodes": nn, "ndof": ndof, "nnz": nnz, "pruned": list(pruned), "tuning": tuning,
                        "l2": "inputs larger than L2 (K+M values alone are %.0f MB)" % (2 * nnz * 8 / 1e6),
                        "setup_s": setup_s, "parallelism": f"replicas x{world}"},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "widened": widened, "configs": configs,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "dfl": dfl, "widened": widened,
+            "configs": configs,
             "gpu_launches": 3 * args.steps, "adjoint": adjoint, "batched": batched,
         }
         print(json.dumps(line), flush=True)

@@ -1,24 +1,39 @@
 // proxgpu/builder.hpp — header-only C++20 drop-in for proxpde's assembly call surface,
 // running on the GB300 engine through its C ABI (include/pxg.h, libpxg.so).
 //
-// The names and the call sequence follow proxpde (include/builder.hpp:12-391 and the
-// Assembly* types of include/assembly_lhs.hpp / assembly_rhs.hpp):
+// The names and the call sequence follow proxpde (include/builder.hpp:12-391, the
+// Assembly* types of include/assembly_lhs.hpp / assembly_rhs.hpp, and the setup and
+// solve calls of its tests, e.g. test/poisson3dhex.cpp:20-104):
 //
-//   auto mesh = proxgpu::buildHyperCube<proxgpu::Hexahedron>(n);       // mesh.hpp:385-421
-//   proxgpu::FESpace<proxgpu::Hexahedron, 1> feSpace{mesh};            // fespace.hpp:27-193
-//   auto bcs = std::vector{proxgpu::BCEss{feSpace, proxgpu::side::LEFT},
-//                          proxgpu::BCEss{feSpace, proxgpu::side::BOTTOM}};
-//   proxgpu::Builder builder{feSpace};                                 // builder.hpp:19
-//   builder.buildLhs(std::tuple{proxgpu::AssemblyStiffness(1.0, feSpace)}, bcs);
-//   builder.buildRhs(std::tuple{proxgpu::AssemblyRhsAnalytic(PXG_FN_POISSON_RHS, feSpace)}, bcs);
+//   using namespace proxgpu;
+//   using Mesh_T = Mesh<Hexahedron>;
+//   using FESpace_T = FESpace<Mesh_T, LagrangeFE<Hexahedron, 1>::RefFE_T,
+//                             LagrangeFE<Hexahedron, 1>::RecommendedQR>;
+//   std::unique_ptr<Mesh_T> mesh{new Mesh_T};
+//   buildHyperCube(*mesh, {0., 0., 0.}, {1., 1., 1.}, {n, n, n});      // mesh.hpp:385-421
+//   FESpace_T feSpace{*mesh};                                          // fespace.hpp:27-193
+//   auto bcLeft = BCEss{feSpace, side::LEFT};
+//   bcLeft << [](Vec3 const &) { return 0.; };                         // bc.hpp:63
+//   Builder builder{feSpace.dof.size};                                 // builder.hpp:19
+//   builder.buildLhs(std::tuple{AssemblyStiffness(1.0, feSpace)}, bcs);
+//   builder.buildRhs(std::tuple{AssemblyRhsAnalytic(rhs, feSpace)}, bcs);  // any f(Vec3)
 //   builder.closeMatrix();
-//   builder.A (CSR arrays on the host), builder.b
+//   LUSolver solver;                                                   // sparse_matrix.hpp:44
+//   solver.analyzePattern(builder.A);
+//   solver.factorize(builder.A);
+//   sol.data = solver.solve(builder.b);
 //
-// Differences from proxpde, all forced by running on a GPU:
-//  - right-hand sides are device functions chosen by id (pxg_fn) instead of a host
-//    std::function; unrecognised assembly types do not compile (no CPU fallback);
+// Differences from proxpde, all forced by running on a GPU or by what the engine
+// replaces:
+//  - a host function rhs (std::function or lambda) is evaluated on the host at the
+//    quadrature points the device reports (pxg_get_qpoints) and integrated on the
+//    device; device functions chosen by id (pxg_fn) are the faster form; unrecognised
+//    assembly types do not compile (no CPU fallback);
 //  - A is returned as CSR arrays; proxpde's default ClmMajor storage is CSC, and for
 //    the symmetric matrices assembled here the CSC arrays are the same arrays;
+//  - LUSolver is the device Jacobi-preconditioned CG (pxg_cg) behind UmfPackLU's
+//    analyzePattern / factorize / solve, to a relative residual of 1e-14 by default;
+//  - Vec is a std::vector<double> with the few Eigen operations the tests use;
 //  - errors throw proxgpu::Error (carrying the pxg_status) instead of aborting.
 #pragma once
 
@@ -26,6 +41,8 @@
 #include <array>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -101,30 +118,35 @@ struct Mesh
   int64_t nelem() const { return (int64_t)conn.size() / Elem::numPts; }
 };
 
-// buildCube on [0,1]^3 with n^3 cubes (src/mesh.cpp:355-534): hexahedra, or 5
-// tetrahedra per cube alternating with the parity of (i + j + k).
+// buildHyperCube(mesh, origin, length, {nx, ny, nz}) (include/mesh.hpp:385-421, with
+// buildCube of src/mesh.cpp:355-534): the box origin + [0, length] split into
+// nx x ny x nz cubes, node (i, j, k) at id i + (nx+1) j + (nx+1)(ny+1) k; hexahedra, or
+// 5 tetrahedra per cube alternating with the parity of (i + j + k).
 template <typename Elem>
-Mesh<Elem> buildHyperCube(int n)
+void buildHyperCube(Mesh<Elem> & m, Vec3 const & origin, Vec3 const & length, std::array<uint32_t, 3> const & n)
 {
-  Mesh<Elem> m;
-  int const np = n + 1;
-  double const h = 1.0 / n;
-  m.xyz.resize((size_t)np * np * np * 3);
-  for (int k = 0; k < np; ++k)
-    for (int j = 0; j < np; ++j)
-      for (int i = 0; i < np; ++i)
+  if (n[0] == 0 || n[1] == 0 || n[2] == 0)
+    throw Error(PXG_ERR_INVALID_ARG, "buildHyperCube: zero elements along an axis");
+  uint32_t const nx = n[0], ny = n[1], nz = n[2];
+  uint32_t const px = nx + 1, py = ny + 1, pz = nz + 1;
+  double const h[3] = {length(0) / nx, length(1) / ny, length(2) / nz};
+  m.xyz.assign((size_t)px * py * pz * 3, 0.);
+  m.conn.clear();
+  for (uint32_t k = 0; k < pz; ++k)
+    for (uint32_t j = 0; j < py; ++j)
+      for (uint32_t i = 0; i < px; ++i)
       {
-        size_t const id = i + (size_t)np * j + (size_t)np * np * k;
-        m.xyz[3 * id] = 0. + i * h;
-        m.xyz[3 * id + 1] = 0. + j * h;
-        m.xyz[3 * id + 2] = 0. + k * h;
+        size_t const id = i + (size_t)px * j + (size_t)px * py * k;
+        m.xyz[3 * id] = origin(0) + i * h[0];
+        m.xyz[3 * id + 1] = origin(1) + j * h[1];
+        m.xyz[3 * id + 2] = origin(2) + k * h[2];
       }
-  uint32_t const dx = 1, dy = np, dz = np * np;
-  for (int k = 0; k < n; ++k)
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < n; ++i)
+  uint32_t const dx = 1, dy = px, dz = px * py;
+  for (uint32_t k = 0; k < nz; ++k)
+    for (uint32_t j = 0; j < ny; ++j)
+      for (uint32_t i = 0; i < nx; ++i)
       {
-        uint32_t const b = i + j * np + k * np * np;
+        uint32_t const b = i + j * dy + k * dz;
         if constexpr (std::is_same_v<Elem, Hexahedron>)
         {
           for (uint32_t v : {b, b + dx, b + dx + dy, b + dy, b + dz, b + dx + dz, b + dx + dy + dz, b + dy + dz})
@@ -148,18 +170,82 @@ Mesh<Elem> buildHyperCube(int n)
               m.conn.push_back(v);
         }
       }
-  return m;
 }
 
-// buildHyperCube(mesh, origin, length, {n, n, n}) (include/mesh.hpp:385-421): the cube
-// above scaled to the box origin + [0, length]
+// the unit cube with n^3 cubes, and the box origin + [0, length] with n^3 cubes
+template <typename Elem>
+Mesh<Elem> buildHyperCube(int n)
+{
+  Mesh<Elem> m;
+  buildHyperCube(m, Vec3(0., 0., 0.), Vec3(1., 1., 1.), {(uint32_t)n, (uint32_t)n, (uint32_t)n});
+  return m;
+}
 template <typename Elem>
 Mesh<Elem> buildHyperCube(std::array<double, 3> const & origin, std::array<double, 3> const & length, int n)
 {
-  Mesh<Elem> m = buildHyperCube<Elem>(n);
-  for (size_t k = 0; k < m.xyz.size(); ++k)
-    m.xyz[k] = origin[k % 3] + m.xyz[k] * length[k % 3];
+  Mesh<Elem> m;
+  buildHyperCube(m, Vec3(origin[0], origin[1], origin[2]), Vec3(length[0], length[1], length[2]),
+                 {(uint32_t)n, (uint32_t)n, (uint32_t)n});
   return m;
+}
+
+// Vec (Eigen::VectorXd in proxpde, include/def.hpp:157-160) with the operations the
+// tests use, and Var (a named vector, include/var.hpp:14-52)
+struct Vec : std::vector<double>
+{
+  using std::vector<double>::vector;
+  Vec(std::vector<double> v): std::vector<double>(std::move(v)) {}
+  double norm() const
+  {
+    double s = 0.;
+    for (double x: *this)
+      s += x * x;
+    return std::sqrt(s);
+  }
+  Vec operator-(Vec const & o) const
+  {
+    if (o.size() != size())
+      throw Error(PXG_ERR_INVALID_ARG, "Vec: sizes differ");
+    Vec r(size());
+    for (size_t k = 0; k < size(); ++k)
+      r[k] = (*this)[k] - o[k];
+    return r;
+  }
+  Vec operator+(Vec const & o) const
+  {
+    if (o.size() != size())
+      throw Error(PXG_ERR_INVALID_ARG, "Vec: sizes differ");
+    Vec r(size());
+    for (size_t k = 0; k < size(); ++k)
+      r[k] = (*this)[k] + o[k];
+    return r;
+  }
+};
+struct Var
+{
+  std::string name;
+  Vec data;
+  explicit Var(std::string n, size_t size = 0): name(std::move(n)), data(size, 0.0) {}
+};
+using scalarFun_T = std::function<double(Vec3 const &)>;
+using vectorFun_T = std::function<Vec3(Vec3 const &)>;
+
+// checkError (include/def.hpp:357-385): each error within tol of its expected value;
+// returns the failure bitset (0 = pass), printing each comparison
+inline int checkError(std::vector<double> const & errors, std::vector<double> const & expected, double tol = 1.e-12)
+{
+  if (errors.size() != expected.size())
+    throw Error(PXG_ERR_INVALID_ARG, "checkError: sizes differ");
+  int fails = 0;
+  for (size_t k = 0; k < errors.size(); ++k)
+  {
+    bool const ok = std::fabs(errors[k] - expected[k]) < tol;
+    std::printf("error: %.16e, expected: %.16e, difference: %.3e %s\n", errors[k], expected[k],
+                std::fabs(errors[k] - expected[k]), ok ? "ok" : "FAIL");
+    if (!ok)
+      fails |= 1 << k;
+  }
+  return fails;
 }
 
 // Device array owned through the C ABI.
@@ -204,12 +290,13 @@ struct DeviceArray
   }
 };
 
-// FESpace<Mesh, LagrangeFE<Elem, Order>::RefFE_T, RecommendedQR> on the device: the
-// mesh, the first-touch DOF map and the CSR pattern live in one engine context.
-// Dim components (BLOCK ordering) and the quadrature of order QrOrder make
-// FESpace<Mesh, RefFE, QR, Dim>; offset is the space's offset in a global system.
+// A Lagrange space on the device: the mesh, the first-touch DOF map and the CSR
+// pattern live in one engine context.  Elem and Order give the reference element, Dim
+// components (BLOCK ordering), QrOrder the order of the element type whose quadrature
+// rule the space uses; offset is the space's offset in a global system.  Users write
+// FESpace<Mesh_T, RefFE_T, QR_T, Dim> (below), as in proxpde.
 template <typename Elem, int Order, int Dim = 1, int QrOrder = Order>
-struct FESpace
+struct FESpaceImpl
 {
   static constexpr int typeOf(int order)
   {
@@ -229,7 +316,7 @@ struct FESpace
   int64_t nelem = 0;
   double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.}; // bounding box of the mesh
 
-  explicit FESpace(Mesh<Elem> const & m, int64_t off = 0, int device = 0): offset(off), nelem(m.nelem())
+  explicit FESpaceImpl(Mesh<Elem> const & m, int64_t off = 0, int device = 0): offset(off), nelem(m.nelem())
   {
     check(pxg_create(&ctx, device), nullptr, "pxg_create");
     check(pxg_set_mesh(ctx, elemType, m.xyz.data(), m.nnodes(), m.conn.data(), m.nelem(), PXG_MEM_HOST), ctx,
@@ -248,9 +335,9 @@ struct FESpace
     double const len[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
     check(pxg_mark_facets_box(ctx, lo, len), ctx, "pxg_mark_facets_box");
   }
-  FESpace(FESpace const &) = delete;
-  FESpace & operator=(FESpace const &) = delete;
-  ~FESpace()
+  FESpaceImpl(FESpaceImpl const &) = delete;
+  FESpaceImpl & operator=(FESpaceImpl const &) = delete;
+  ~FESpaceImpl()
   {
     if (ctx)
       pxg_destroy(ctx);
@@ -264,7 +351,74 @@ struct FESpace
     check(pxg_interpolate(ctx, fn, coef, v.p, nullptr), ctx, "pxg_interpolate");
     return v.host();
   }
+  // CurFE::qpoint of every element and quadrature point (nelem x nq x 3)
+  std::vector<double> qpoints() const
+  {
+    int const nq = elemType == PXG_P1TET ? 4 : elemType == PXG_P2TET ? 11 : elemType == PXG_Q1HEX ? 8 : 27;
+    std::vector<double> q((size_t)nelem * nq * 3);
+    check(pxg_get_qpoints(ctx, q.data(), PXG_MEM_HOST, nullptr), ctx, "pxg_get_qpoints");
+    return q;
+  }
 };
+
+// Reference elements and quadrature rules as type tags, with proxpde's names:
+// LagrangeFE<Elem, Order>::RefFE_T / ::RecommendedQR (include/fe.hpp:96-131),
+// GaussQR<Elem, points> (include/qr.hpp), RefTetrahedronP1 ... (include/reffe.hpp).
+template <typename Elem, int Order>
+struct RefLagrange
+{
+  using Elem_T = Elem;
+  static constexpr int order = Order;
+};
+template <typename Elem, int NumPts>
+struct GaussQR
+{
+  static_assert(NumPts == 4 || NumPts == 11 || NumPts == 8 || NumPts == 27, "rules of the Lagrange elements only");
+  using Elem_T = Elem;
+  static constexpr int order = (NumPts == 4 || NumPts == 8) ? 1 : 2; // the element order it belongs to
+};
+template <typename Elem, int Order>
+struct LagrangeFE
+{
+  static_assert(Order == 1 || Order == 2, "P1/P2 tetrahedra and Q1/Q2 hexahedra");
+  using RefFE_T = RefLagrange<Elem, Order>;
+  using RecommendedQR =
+      GaussQR<Elem, std::is_same_v<Elem, Tetrahedron> ? (Order == 1 ? 4 : 11) : (Order == 1 ? 8 : 27)>;
+};
+using RefTetrahedronP1 = RefLagrange<Tetrahedron, 1>;
+using RefTetrahedronP2 = RefLagrange<Tetrahedron, 2>;
+using RefHexahedronQ1 = RefLagrange<Hexahedron, 1>;
+using RefHexahedronQ2 = RefLagrange<Hexahedron, 2>;
+
+// FESpace<Mesh_T, RefFE_T, QR_T, Dim> (include/fespace.hpp:15-60)
+template <typename Mesh_T, typename RefFE_T, typename QR_T, unsigned Dim = 1>
+struct FESpace: FESpaceImpl<typename RefFE_T::Elem_T, RefFE_T::order, (int)Dim, QR_T::order>
+{
+  static_assert(std::is_same_v<Mesh_T, Mesh<typename RefFE_T::Elem_T>>, "the mesh and the element must match");
+  static_assert(std::is_same_v<typename QR_T::Elem_T, typename RefFE_T::Elem_T>, "the rule and the element must match");
+  using FESpaceImpl<typename RefFE_T::Elem_T, RefFE_T::order, (int)Dim, QR_T::order>::FESpaceImpl;
+};
+
+// interpolateAnalyticFunction(f, feSpace, v) (include/fespace.hpp:195-271) for a host
+// function of the point: f at the DOF points (from the device); a vector space takes
+// f returning Vec3 and fills every component (BLOCK ordering)
+template <typename F, typename FE, typename = std::enable_if_t<std::is_invocable_v<F const &, Vec3 const &>>>
+void interpolateAnalyticFunction(F const & f, FE const & fe, std::vector<double> & v)
+{
+  std::vector<double> const x = fe.interpolate(PXG_FN_COORD_X), y = fe.interpolate(PXG_FN_COORD_Y),
+                            z = fe.interpolate(PXG_FN_COORD_Z);
+  size_t const n = x.size();
+  v.assign(n * FE::dim, 0.0);
+  for (size_t k = 0; k < n; ++k)
+  {
+    auto const r = f(Vec3(x[k], y[k], z[k]));
+    if constexpr (std::is_arithmetic_v<std::decay_t<decltype(r)>>)
+      v[k] = r;
+    else
+      for (int c = 0; c < FE::dim; ++c)
+        v[k + c * n] = r(c);
+  }
+}
 
 // BCEss (include/bc.hpp:81-97) on the DOFs of the boundary facets with a marker, or on
 // an explicit list.  Marker with a constant on a scalar space: the constrained set is
@@ -299,7 +453,29 @@ struct BCEss
   }
   BCEss(std::vector<uint32_t> d, std::vector<double> v): dofs(std::move(d)), values(std::move(v)) {}
 
+  // BCEss << f (include/bc.hpp:63-79): new values, f at the constrained DOFs' points
+  // (scalar f, or Vec3 f whose component c goes to the DOFs of component c)
+  template <typename F, typename = std::enable_if_t<std::is_invocable_v<F const &, Vec3 const &>>>
+  BCEss & operator<<(F const & fun)
+  {
+    if (pts.size() != 3 * dofs.size())
+      throw Error(PXG_ERR_INVALID_ARG, "BCEss <<: the condition was given as an explicit DOF list");
+    for (size_t k = 0; k < dofs.size(); ++k)
+    {
+      auto const r = fun(Vec3(pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]));
+      if constexpr (std::is_arithmetic_v<std::decay_t<decltype(r)>>)
+        values[k] = r;
+      else
+        values[k] = r(comp[k]);
+    }
+    marker = side::NONE; // the values are a function now: the explicit list applies
+    return *this;
+  }
+
 private:
+  std::vector<double> pts; // the constrained DOFs' points
+  std::vector<int> comp;   // and components
+
   // the DOFs on the marker's plane of the box (markFacetsCube), for every component
   template <typename FE, typename F>
   void collect(FE const & fe, int m, F const & fun, std::vector<int> comps)
@@ -325,6 +501,8 @@ private:
             val = r(c);
           dofs.push_back((uint32_t)(k + (size_t)c * xa.size()));
           values.push_back(val);
+          pts.insert(pts.end(), {x[k], y[k], z[k]});
+          comp.push_back(c);
         }
   }
 };
@@ -368,20 +546,49 @@ struct AssemblyMassFE
   AssemblyMassFE(std::vector<double> const & k, FE const & fe): coefP0(&k), feSpace(&fe) {}
 };
 
-// AssemblyRhsAnalytic(f, feSpace, comps) (include/assembly_rhs.hpp:34-91) with device
-// functions chosen by id.  A scalar space takes one id; a vector space takes one id
-// and one coefficient per component (the components of the reference's vector
-// function), and only the listed components (default: all) get a load, component c
-// into block c.
+// AssemblyRhsAnalytic(f, feSpace, comps) (include/assembly_rhs.hpp:34-91).  f is any
+// function of the point, as in the reference (a lambda or std::function returning a
+// double on a scalar space, a Vec3 on a vector space): it is evaluated on the host at
+// the quadrature points the device reports, and the values are integrated on the
+// device (rhs kind 3).  f may also be a device function chosen by id (pxg_fn): one id
+// on a scalar space, one id and one coefficient per component on a vector space.  Only
+// the listed components (default: all) get a load, component c into block c.
 template <typename FE>
 struct AssemblyRhsAnalytic
 {
   int fn;
   double coef;
   FE const * feSpace;
-  std::vector<int> fns;      // per component
+  std::vector<int> fns;      // per component (-1: values at the quadrature points)
   std::vector<double> coefs; // per component
   std::vector<int> comps;
+  std::vector<std::vector<double>> qvals; // per component: f at the quadrature points
+  template <typename F, typename = std::enable_if_t<std::is_invocable_v<F const &, Vec3 const &>>>
+  AssemblyRhsAnalytic(F const & f, FE const & fe, std::vector<int> cmp = {}):
+      fn(-1), coef(1.0), feSpace(&fe), fns(FE::dim, -1), coefs(FE::dim, 1.0), comps(std::move(cmp))
+  {
+    if (comps.empty())
+      for (int d = 0; d < FE::dim; ++d)
+        comps.push_back(d);
+    for (int d: comps)
+      if (d < 0 || d >= FE::dim)
+        throw Error(PXG_ERR_INVALID_ARG, "AssemblyRhsAnalytic: component out of range");
+    std::vector<double> const qp = fe.qpoints();
+    size_t const n = qp.size() / 3;
+    qvals.assign(FE::dim, std::vector<double>(n));
+    for (size_t k = 0; k < n; ++k)
+    {
+      auto const r = f(Vec3(qp[3 * k], qp[3 * k + 1], qp[3 * k + 2]));
+      if constexpr (std::is_arithmetic_v<std::decay_t<decltype(r)>>)
+      {
+        static_assert(FE::dim == 1, "a vector space takes a function returning Vec3");
+        qvals[0][k] = r;
+      }
+      else
+        for (int c = 0; c < FE::dim; ++c)
+          qvals[(size_t)c][k] = r(c);
+    }
+  }
   AssemblyRhsAnalytic(int f, FE const & fe, double c = 1.0): fn(f), coef(c), feSpace(&fe), fns{f}, coefs{c}, comps{0}
   {
     static_assert(FE::dim == 1, "this ctor is available only for scalar fe spaces.");
@@ -454,14 +661,70 @@ struct AssemblyDiv
   static constexpr int kind = PXG_OP_DIV;
 };
 
-// CSR matrix on the host
+// CSR matrix on the host; ctx is the engine context (GPU) that assembled it
 struct CsrMatrix
 {
   int64_t rows = 0, cols = 0;
   std::vector<int32_t> outer; // row_ptr
   std::vector<int32_t> inner; // col_idx
   std::vector<double> values;
+  pxg_ctx * ctx = nullptr;
   int64_t nonZeros() const { return (int64_t)values.size(); }
+};
+
+// UmfPackLU's interface as the tests use it (include/sparse_matrix.hpp:44:
+// analyzePattern, factorize, solve) over the engine's device Jacobi-preconditioned CG
+// (pxg_cg): factorize copies the matrix to the GPU that assembled it, and each solve
+// runs the CG from x = 0 to the relative residual rtol (1e-14 by default), throwing
+// PXG_ERR_NOT_CONVERGED if it stops at maxIter.  The CG needs a symmetric positive
+// definite matrix, which a direct LU does not; iterations and relRes report the last
+// solve.
+struct LUSolver
+{
+  double rtol = 1e-14;
+  int maxIter = 0; // 0: 10 * rows + 1000
+  int iterations = 0;
+  double relRes = 0.;
+
+  void analyzePattern(CsrMatrix const & A)
+  {
+    if (!A.ctx || A.rows != A.cols || (int64_t)A.outer.size() != A.rows + 1)
+      throw Error(PXG_ERR_INVALID_ARG, "LUSolver: a square matrix closed by a Builder is needed");
+    ctx = A.ctx;
+    n = A.rows;
+  }
+  void factorize(CsrMatrix const & A)
+  {
+    if (A.ctx != ctx || A.rows != n)
+      throw Error(PXG_ERR_INVALID_ARG, "LUSolver: factorize a matrix of the analysed pattern");
+    rp = DeviceArray<int32_t>(ctx, A.outer.size());
+    ci = DeviceArray<int32_t>(ctx, std::max<size_t>(A.inner.size(), 1));
+    va = DeviceArray<double>(ctx, std::max<size_t>(A.values.size(), 1));
+    check(pxg_memcpy(ctx, rp.p, A.outer.data(), A.outer.size() * 4, 0, nullptr), ctx, "pxg_memcpy");
+    check(pxg_memcpy(ctx, ci.p, A.inner.data(), A.inner.size() * 4, 0, nullptr), ctx, "pxg_memcpy");
+    check(pxg_memcpy(ctx, va.p, A.values.data(), A.values.size() * 8, 0, nullptr), ctx, "pxg_memcpy");
+  }
+  void compute(CsrMatrix const & A)
+  {
+    analyzePattern(A);
+    factorize(A);
+  }
+  Vec solve(std::vector<double> const & b)
+  {
+    if (!rp.p || (int64_t)b.size() != n)
+      throw Error(PXG_ERR_INVALID_ARG, "LUSolver: factorize first; b must have one value per row");
+    DeviceArray<double> bd(ctx, (size_t)n), xd(ctx, (size_t)n);
+    check(pxg_memcpy(ctx, bd.p, b.data(), (size_t)n * 8, 0, nullptr), ctx, "pxg_memcpy");
+    int const mi = maxIter > 0 ? maxIter : (int)std::min<int64_t>(10 * n + 1000, 1 << 30);
+    check(pxg_cg(ctx, rp.p, ci.p, va.p, n, bd.p, xd.p, rtol, mi, &iterations, &relRes, nullptr), ctx, "pxg_cg");
+    return Vec(xd.host());
+  }
+
+private:
+  pxg_ctx * ctx = nullptr;
+  int64_t n = 0;
+  DeviceArray<int32_t> rp, ci;
+  DeviceArray<double> va;
 };
 
 template <typename FE, StorageType Storage = StorageType::ClmMajor>
@@ -509,6 +772,7 @@ struct Builder
     int64_t nnz = 0;
     check(pxg_close_matrix(fe.ctx, vals.p, rp.p, ci.p, vo.p, &nnz, nullptr), fe.ctx, "pxg_close_matrix");
     A.rows = A.cols = n;
+    A.ctx = fe.ctx;
     A.outer = rp.host();
     A.inner = ci.host();
     A.inner.resize((size_t)nnz);
@@ -606,6 +870,16 @@ private:
   template <typename X>
   void addRhs(AssemblyRhsAnalytic<X> const & a, int bc)
   {
+    if (!a.qvals.empty())
+    {
+      // a host function: its values at the quadrature points, integrated on the device
+      DeviceArray<double> f(fe.ctx, a.qvals[0].size());
+      check(pxg_memcpy(fe.ctx, f.p, a.qvals[0].data(), f.n * sizeof(double), 0, nullptr), fe.ctx, "pxg_memcpy");
+      pxg_rhs_op r{3, 0, a.coef, f.p, bc};
+      check(pxg_assemble(fe.ctx, nullptr, nullptr, nullptr, nullptr, &r, bDev.p, PXG_ACCUMULATE, nullptr), fe.ctx,
+            "pxg_assemble");
+      return; // f is released here; freeing device memory waits for the assembly that reads it
+    }
     pxg_rhs_op r{1, a.fn, a.coef, nullptr, bc};
     check(pxg_assemble(fe.ctx, nullptr, nullptr, nullptr, nullptr, &r, bDev.p, PXG_ACCUMULATE, nullptr), fe.ctx,
           "pxg_assemble");
@@ -750,12 +1024,12 @@ struct Builder<void, Storage>
         }
         check(pxg_set_bc(sp.ctx, d.data(), v.data(), (int64_t)d.size(), diag, PXG_MEM_HOST), sp.ctx, "pxg_set_bc");
         DeviceArray<double> f;
+        size_t const fn = part.kind == 3 ? (size_t)sp.nelem * sp.nq : (size_t)sp.ndof;
+        size_t const foff = part.kind == 3 ? 0 : (size_t)part.fieldComp * sp.ndof;
         if (part.field)
-          f = DeviceArray<double>(sp.ctx, (size_t)sp.ndof);
+          f = DeviceArray<double>(sp.ctx, fn);
         if (part.field)
-          check(pxg_memcpy(sp.ctx, f.p, part.field + part.fieldComp * sp.ndof, (size_t)sp.ndof * sizeof(double), 0,
-                           nullptr),
-                sp.ctx, "pxg_memcpy");
+          check(pxg_memcpy(sp.ctx, f.p, part.field + foff, fn * sizeof(double), 0, nullptr), sp.ctx, "pxg_memcpy");
         pxg_rhs_op op{part.kind, part.fn, part.coef, f.p, r.bcs.empty() ? 0 : 1};
         check(pxg_assemble(sp.ctx, nullptr, nullptr, nullptr, nullptr, &op, bd.p + sp.offset + lo, PXG_ACCUMULATE,
                            nullptr),
@@ -763,15 +1037,12 @@ struct Builder<void, Storage>
         // f is released here; freeing device memory waits for the assembly that reads it
       }
     }
-    int32_t const * rp = nullptr;
-    int32_t const * ci = nullptr;
-    check(pxg_sys_pattern_device(S, &rp, &ci), c0, "pxg_sys_pattern_device");
     DeviceArray<int32_t> rpo(c0, (size_t)ntot + 1), cio(c0, (size_t)nnz);
     DeviceArray<double> vo(c0, (size_t)nnz);
     int64_t kept = 0;
-    check(pxg_prune_csr_noalloc(rp, ci, vals.p, ntot, rpo.p, cio.p, vo.p, &kept, nullptr), c0,
-          "pxg_prune_csr_noalloc");
+    check(pxg_sys_close_matrix(S, vals.p, rpo.p, cio.p, vo.p, &kept, nullptr), c0, "pxg_sys_close_matrix");
     A.rows = A.cols = ntot;
+    A.ctx = c0;
     A.outer = rpo.host();
     A.inner = cio.host();
     A.inner.resize((size_t)kept);
@@ -788,6 +1059,8 @@ private:
     pxg_ctx * ctx;
     int dim, qr;
     int64_t offset, ndof;
+    int64_t nelem;
+    int nq; // quadrature points per element of the element type's own rule
   };
   struct Call
   {
@@ -800,8 +1073,8 @@ private:
   {
     int block, kind, fn;
     double coef;
-    double const * field; // projection: the whole field on the host, else null
-    int fieldComp;
+    double const * field; // projection: the whole field on the host; kind 3: the values
+    int fieldComp;        // at the quadrature points; else null
   };
   struct RhsCall
   {
@@ -826,7 +1099,10 @@ private:
     checkRule<X>();
     RhsCall r{spaceOf(*a.feSpace), {}, bcs};
     for (int c: a.comps)
-      r.parts.push_back(RhsPart{c, 1, a.fns[(size_t)c], a.coefs[(size_t)c], nullptr, 0});
+      if (a.qvals.empty())
+        r.parts.push_back(RhsPart{c, 1, a.fns[(size_t)c], a.coefs[(size_t)c], nullptr, 0});
+      else
+        r.parts.push_back(RhsPart{c, 3, 0, a.coefs[(size_t)c], a.qvals[(size_t)c].data(), c});
     rhsCalls.push_back(std::move(r));
   }
   template <typename X>
@@ -845,7 +1121,8 @@ private:
     for (size_t k = 0; k < spaces.size(); ++k)
       if (spaces[k].ctx == fe.ctx)
         return (int)k;
-    spaces.push_back(Space{fe.ctx, FE::dim, FE::qrType, fe.offset, fe.dof.size});
+    int const nq = FE::elemType == PXG_P1TET ? 4 : FE::elemType == PXG_P2TET ? 11 : FE::elemType == PXG_Q1HEX ? 8 : 27;
+    spaces.push_back(Space{fe.ctx, FE::dim, FE::qrType, fe.offset, fe.dof.size, fe.nelem, nq});
     return (int)spaces.size() - 1;
   }
   template <typename FE>

@@ -102,6 +102,11 @@ typedef struct pxg_lhs_op
  *           (include/assembly_rhs.hpp:34-91), f evaluated at CurFE::qpoint
  *        2: AssemblyS2SProjection(coef, field) of a DOF vector on the same space
  *           (include/assembly_rhs.hpp:93-163); `field` is a device pointer (ndof)
+ *        3: AssemblyRhsAnalytic with any function, evaluated by the caller at the
+ *           quadrature points that pxg_get_qpoints returns: `field` is a device
+ *           pointer to nelem x nq values f(qpoint) (element-major), scaled by `coef`
+ *           (the reference's host std::function, assembly_rhs.hpp:50-59, cannot run on
+ *           the device, so the caller evaluates it there)
  *   apply_bc  zero constrained rows (C*Fe, builder.hpp:319-347). */
 typedef struct pxg_rhs_op
 {
@@ -245,6 +250,11 @@ pxg_status pxg_sys_create(pxg_sys ** sys, pxg_ctx * const * spaces, const int * 
 pxg_status pxg_sys_destroy(pxg_sys * sys);
 pxg_status pxg_sys_get_pattern(pxg_sys * sys, int32_t * row_ptr, int32_t * col_idx);
 pxg_status pxg_sys_pattern_device(pxg_sys * sys, const int32_t ** row_ptr, const int32_t ** col_idx);
+/* Builder::closeMatrix on the system's pattern (pxg_close_matrix for a system): the
+ * pruned CSR of vals (row_ptr[ntot+1], col_idx and vals_out with capacity nnz, device
+ * pointers) and its entry count; scratch is allocated on the first space's device. */
+pxg_status pxg_sys_close_matrix(pxg_sys * sys, const double * vals, int32_t * row_ptr, int32_t * col_idx,
+                                double * vals_out, int64_t * nnz_out, void * stream);
 /* Dirichlet data of one space over its component DOFs (host arrays; the last value wins). */
 pxg_status pxg_sys_set_bc(pxg_sys * sys, int space, const uint32_t * dofs, const double * vals, int64_t n,
                           double diag);
@@ -276,6 +286,19 @@ pxg_status pxg_prune_count_device(pxg_ctx * ctx, const double * vals, int64_t * 
  * 512 (Q1 hexahedra), 128 (Q2 hexahedra).  PXG_SCATTER_COLOUR builds the element
  * colouring on the first use (not during a stream capture). */
 pxg_status pxg_set_scatter(pxg_ctx * ctx, int scatter, int threads);
+/* Arithmetic of the element kernels.  The reference computes geometry, local matrices
+ * and sums in double (FVec/FMat, include/def.hpp:157-160); PXG_ARITH_FP64, the
+ * default, does the same: every value is formed by IEEE binary64 operations.
+ * PXG_ARITH_DFL is an opt-in alternative with a narrower significand: the geometry and
+ * the local matrices run as unevaluated pairs of floats (about 48 bits) on the FP32
+ * pipes, and only the coordinate differences, the final sums and the reductions into
+ * the outputs stay FP64.  Changing it resets the threads per block to the default. */
+typedef enum pxg_arith
+{
+  PXG_ARITH_FP64 = 0,
+  PXG_ARITH_DFL = 1
+} pxg_arith;
+pxg_status pxg_set_arithmetic(pxg_ctx * ctx, int arith);
 /* Element colouring of the colour-ordered scatter (built if needed): the number of
  * colour classes, and optionally the elements in colour order (nelem entries) and the
  * class offsets (ncolours + 1 entries), host arrays. */
@@ -290,6 +313,13 @@ pxg_status pxg_autotune(pxg_ctx * ctx, const pxg_lhs_op * op0, const pxg_lhs_op 
 pxg_status pxg_close_matrix(pxg_ctx * ctx, const double * vals, int32_t * row_ptr,
                             int32_t * col_idx, double * vals_out, int64_t * nnz_out,
                             void * stream);
+
+/* CurFE::qpoint (include/curfe.hpp:80) of every element and quadrature point of the
+ * element type's rule: qpts[(e * nq + q) * 3 + d], nq = 4 / 11 / 8 / 27 for P1 / P2 /
+ * Q1 / Q2, the point origin + J(xi_q) xi_q with origin the first vertex (tetrahedra) or
+ * the vertex average (hexahedra, include/geo.hpp:721-728).  mem: where qpts lives
+ * (host copies synchronise the stream).  The points rhs kind 3 expects its values at. */
+pxg_status pxg_get_qpoints(pxg_ctx * ctx, double * qpts, int mem, void * stream);
 
 /* Lagrange interpolation of an analytic function at the DOF points
  * (interpolateAnalyticFunction, include/fespace.hpp:195-271): v[ndof], device. */
@@ -351,6 +381,13 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, const pxg_rhs_op 
                              double * losses, double * const * grads, int * iters, int use_graph,
                              void * stream);
 
+/* -------------------------------------------------------------- measurement
+ * No counterpart in proxpde: the FP64 FMA rate of a device (FMAs per second, one FMA
+ * = two floating-point operations), from an event-timed kernel of independent FMA
+ * chains; the ceiling of the FP64-bound element kernels, reported beside their time.
+ * ms (may be NULL) receives the timed launch's duration. */
+pxg_status pxg_fp64_rate(int device, double * fma_per_s, double * ms);
+
 /* ----------------------------------------------------- allocation-free prune
  * No counterpart in proxpde: an allocation-free variant of pxg_close_matrix's
  * prune/compact for callers that cannot call cudaMalloc (code running where the
@@ -363,9 +400,9 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, const pxg_rhs_op 
  * Builder::closeMatrix's prune(1., 1e-16) does.
  * Limits: nrows <= 4,194,304 (else PXG_ERR_INVALID_ARG); its intermediate data live
  * in one fixed 16.8 MB device array that every GPU loading the library keeps until
- * exit.  The first call on a device looks up that array's address (make it before
- * any stream capture).  Calls that overlap on the GPU share the array and race:
- * serialise them.  It synchronises `stream` to return the count. */
+ * exit.  The first call on a device looks up that array's address.  Calls that
+ * overlap on the GPU share the array and race: serialise them.  Every call
+ * synchronises `stream` to return the count, so it cannot be stream-captured. */
 pxg_status pxg_prune_csr_noalloc(const int32_t * row_ptr, const int32_t * col_idx,
                                  const double * vals, int64_t nrows, int32_t * row_ptr_out,
                                  int32_t * col_idx_out, double * vals_out, int64_t * nnz_out,

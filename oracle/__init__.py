@@ -83,6 +83,7 @@ def lib():
         L.orc_dofmap.restype = C.c_int64
         L.orc_dof_coords.argtypes = [C.c_int, dp, up, C.c_int64, up, dp]
         L.orc_interpolate.argtypes = [C.c_int, dp, up, C.c_int64, up, C.c_int, C.c_double, dp]
+        L.orc_qpoints.argtypes = [C.c_int, dp, up, C.c_int64, dp]
         L.orc_element.argtypes = [C.c_int, dp, up, C.c_int64, C.POINTER(OrcLhs), C.POINTER(OrcRhs), up, dp, dp]
         L.orc_build.argtypes = [
             C.c_int, dp, up, C.c_int64, up, C.c_int64, C.POINTER(OrcLhs), C.POINTER(OrcRhs),
@@ -166,6 +167,15 @@ def dof_coords(t, xyz, conn, em, ndof):
     out = np.zeros((ndof, 3))
     lib().orc_dof_coords(t, _dp(np.ascontiguousarray(xyz)), _up(np.ascontiguousarray(conn, dtype=np.uint32)),
                          conn.shape[0], _up(np.ascontiguousarray(em, dtype=np.uint32)), _dp(out))
+    return out
+
+
+def qpoints(t, xyz, conn):
+    """CurFE::qpoint of every element and quadrature point, (nelem, nq, 3)."""
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    nq = lib().orc_num_qpts(t)
+    out = np.zeros((conn.shape[0], nq, 3))
+    lib().orc_qpoints(t, _dp(np.ascontiguousarray(xyz)), _up(conn), conn.shape[0], _dp(out))
     return out
 
 

@@ -660,6 +660,18 @@ int orc_element(int t, double const * xyz, uint32_t const * conn, int64_t e,
           Fe[i] += fe->JxW[q] * p[i] * f;
       }
     }
+    else if (rhs && rhs->kind == 3)
+    {
+      // AssemblyRhsAnalytic (assembly_rhs.hpp:61-88) with f(qpoint) given: values of
+      // an arbitrary function at this element's CurFE::qpoint, field[e * nq + q]
+      for (int q = 0; q < nq; ++q)
+      {
+        double const f = rhs->c * rhs->field[e * nq + q];
+        double const * p = &fe->phiRef[q * N];
+        for (int i = 0; i < N; ++i)
+          Fe[i] += fe->JxW[q] * p[i] * f;
+      }
+    }
     else if (rhs && rhs->kind == 2)
     {
       // AssemblyS2SProjection (assembly_rhs.hpp:130-159)
@@ -678,6 +690,24 @@ int orc_element(int t, double const * xyz, uint32_t const * conn, int64_t e,
     }
   }
   return 0;
+}
+
+// CurFE::qpoint (curfe.hpp:80) of every element and quadrature point:
+// out[(e * nq + q) * 3 + d]
+void orc_qpoints(int t, double const * xyz, uint32_t const * conn, int64_t nelem, double * out)
+{
+  int const nv = numVerts(t);
+  CurFE fe(t);
+  for (int64_t e = 0; e < nelem; ++e)
+  {
+    double X[8][3];
+    for (int a = 0; a < nv; ++a)
+      for (int d = 0; d < 3; ++d)
+        X[a][d] = xyz[3 * (int64_t)conn[e * nv + a] + d];
+    fe.reinit(X);
+    for (int k = 0; k < fe.nq * 3; ++k)
+      out[e * fe.nq * 3 + k] = fe.qpt[k];
+  }
 }
 
 // ------------------------------------------------------------------ builder

@@ -8,13 +8,14 @@ parity tests) read like proxpde's own tests (e.g. test/poisson3dhex.cpp:46-74):
     bcs = [BCEss(fe, side.LEFT), BCEss(fe, side.BOTTOM)]    # include/bc.hpp:32-306
     builder = Builder(fe)                                   # include/builder.hpp:12-391
     builder.buildLhs((AssemblyStiffness(1.0, fe),), bcs)
-    builder.buildRhs((AssemblyRhsAnalytic(FN_POISSON_RHS, fe),), bcs)
+    builder.buildRhs((AssemblyRhsAnalytic(lambda p: np.sin(p[:, 0]), fe),), bcs)
     builder.closeMatrix()
     builder.A  (scipy CSR on the host) / builder.A_dev (device CSR)  builder.b
 
-Every computation runs on the GPU through libpxg.so (include/pxg.h); there is no CPU
-path.  A host std::function rhs has no device equivalent, so analytic right-hand
-sides are chosen by id (FN_*).
+Every assembly runs on the GPU through libpxg.so (include/pxg.h); there is no CPU
+path.  An analytic right-hand side is either any Python callable, evaluated on the
+host at the quadrature points the device reports and integrated on the device, or one
+of the device's function ids (FN_*), evaluated on the device.
 """
 from __future__ import annotations
 
@@ -30,7 +31,7 @@ __all__ = [
     "AssemblyS2SProjection", "AssemblyProjection", "interpolateAnalyticFunction", "Context", "PxgError",
     "AssemblyTensorStiffness", "AssemblyGrad", "AssemblyDiv",
     "FN_CONST", "FN_SIN3", "FN_POISSON_RHS", "FN_POISSON_EXACT", "P1TET", "P2TET", "Q1HEX", "Q2HEX", "meshgen",
-    "load", "SCATTER_REDUCE", "SCATTER_COLOUR",
+    "load", "SCATTER_REDUCE", "SCATTER_COLOUR", "LUSolver",
 ]
 
 
@@ -360,28 +361,44 @@ def _sys_op(a):
 
 
 class AssemblyRhsAnalytic:
-    """AssemblyRhsAnalytic(f, feSpace, comps) with f chosen by id
-    (include/assembly_rhs.hpp:34-91).
+    """AssemblyRhsAnalytic(f, feSpace, comps) (include/assembly_rhs.hpp:34-91).
 
-    On a scalar space f is one function id.  On a vector space f is one id per
-    component (the components of the reference's vector function), coef one value or one
-    per component, and only the components listed in ``comps`` (default: all) get a
-    load: component c of the load goes to block c (assembly_rhs.hpp:66-73)."""
+    f is any Python callable, as the reference takes any std::function: it gets the
+    (n, 3) array of the space's quadrature points (CurFE::qpoint, from the device) and
+    returns n values (a scalar space) or an (n, dim) array (a vector space); the values
+    go to the device and are integrated there (rhs kind 3).  f may also be one of the
+    device's function ids (pxg_fn, evaluated on the device: the fast path), one per
+    component on a vector space.  coef scales f (one value or one per component), and
+    only the components listed in ``comps`` (default: all) get a load: component c of
+    the load goes to block c (assembly_rhs.hpp:66-73)."""
 
     def __init__(self, fn, fe, coef=1.0, comps=None):
         self.fe = fe
+        coefs = np.broadcast_to(np.asarray(coef, dtype=np.float64), (fe.dim,))
+        comps = list(range(fe.dim)) if comps is None else [int(c) for c in comps]
+        if any(not 0 <= c < fe.dim for c in comps):
+            raise ValueError("AssemblyRhsAnalytic: component out of range")
+        if callable(fn):
+            import torch
+
+            qp = fe.ctx.get_qpoints().reshape(-1, 3)
+            v = np.asarray(fn(qp), dtype=np.float64).reshape(qp.shape[0], -1)
+            if v.shape[1] != fe.dim:
+                raise ValueError(f"AssemblyRhsAnalytic: f returned {v.shape[1]} components, the space has {fe.dim}")
+            dev = f"cuda:{fe.ctx.device}"
+            self.values = [torch.as_tensor(np.ascontiguousarray(v[:, c])).to(dev) for c in range(fe.dim)]
+            self.parts = [(c, {"kind": 3, "coef": float(coefs[c]), "field": self.values[c]}) for c in comps]
+            self.rhs = self.parts[0][1]
+            return
         if fe.dim == 1:
-            if np.ndim(fn) != 0 or comps not in (None, [0], (0,)):
+            if np.ndim(fn) != 0 or comps != [0]:
                 raise ValueError("AssemblyRhsAnalytic: a scalar space takes one function id")
             self.rhs = {"kind": 1, "fn": int(fn), "coef": float(coef)}
             self.parts = [(0, self.rhs)]
             return
-        fns, coefs = np.asarray(fn).reshape(-1), np.broadcast_to(np.asarray(coef, dtype=np.float64), (fe.dim,))
+        fns = np.asarray(fn).reshape(-1)
         if fns.size != fe.dim:
             raise ValueError(f"AssemblyRhsAnalytic: a {fe.dim}-component space takes {fe.dim} function ids")
-        comps = list(range(fe.dim)) if comps is None else [int(c) for c in comps]
-        if any(not 0 <= c < fe.dim for c in comps):
-            raise ValueError("AssemblyRhsAnalytic: component out of range")
         self.parts = [(c, {"kind": 1, "fn": int(fns[c]), "coef": float(coefs[c])}) for c in comps]
 
 
@@ -614,3 +631,47 @@ class Builder:
     def clear(self):
         self.clearLhs()
         self.clearRhs()
+
+
+class LUSolver:
+    """UmfPackLU's interface as proxpde's tests use it (include/sparse_matrix.hpp:44:
+    analyzePattern, factorize, solve) over the engine's device Jacobi-preconditioned CG
+    (pxg_cg) on a Builder's closed matrix: factorize keeps the device CSR
+    (Builder.A_dev), each solve runs the CG from x = 0 to the relative residual rtol
+    (1e-14 by default) and raises PxgError (not converged) at max_iter.  The CG needs a
+    symmetric positive definite matrix, which a direct LU does not.  iterations and
+    rel_res report the last solve."""
+
+    def __init__(self, rtol=1e-14, max_iter=None):
+        self.rtol, self.max_iter = float(rtol), max_iter
+        self.builder = None
+        self.iterations, self.rel_res = 0, 0.0
+
+    def analyzePattern(self, builder):
+        if getattr(builder, "A_dev", None) is None or builder.fe is None:
+            raise PxgError(1, "LUSolver: a scalar Builder closed with closeMatrix is needed")
+        self.builder = builder
+
+    def factorize(self, builder):
+        if builder is not self.builder:
+            raise PxgError(1, "LUSolver: factorize the analysed Builder's matrix")
+        rp, ci, v = builder.A_dev
+        self.A = (rp, ci.contiguous(), v.contiguous())
+
+    def compute(self, builder):
+        self.analyzePattern(builder)
+        self.factorize(builder)
+
+    def solve(self, b):
+        import torch
+
+        rp, ci, v = self.A
+        ctx = self.builder.fe.ctx
+        bd = torch.as_tensor(np.ascontiguousarray(b, dtype=np.float64)).to(rp.device)
+        x = torch.zeros_like(bd)
+        n = bd.numel()
+        mi = self.max_iter or 10 * n + 1000
+        self.iterations, self.rel_res = ctx.cg(rp, ci, v, bd, x, rtol=self.rtol, max_iter=mi)
+        torch.cuda.synchronize()
+        return x.cpu().numpy()
+

@@ -35,6 +35,7 @@ EXPORTS = [
     "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
     "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
+    "pxg_set_arithmetic", "pxg_fp64_rate", "pxg_sys_close_matrix", "pxg_get_qpoints",
 ]
 
 
@@ -77,6 +78,8 @@ class TuneReport(C.Structure):
 
 
 SCATTER_REDUCE, SCATTER_COLOUR = 0, 1
+# arithmetic of the element kernels: IEEE binary64 (default) or double-float (opt-in)
+ARITH_FP64, ARITH_DFL = 0, 1
 SCATTER_NAMES = {SCATTER_REDUCE: "reduce", SCATTER_COLOUR: "colour"}
 
 _lib = None
@@ -112,10 +115,13 @@ def load(path: str = LIB_PATH):
         "pxg_prune_count": ([vp, vp, i64p, vp], C.c_int),
         "pxg_prune_count_device": ([vp, vp, vp, vp], C.c_int),
         "pxg_set_scatter": ([vp, C.c_int, C.c_int], C.c_int),
+        "pxg_set_arithmetic": ([vp, C.c_int], C.c_int),
+        "pxg_fp64_rate": ([C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "pxg_sys_create": ([C.POINTER(vp), vp, vp, vp, C.c_int, i64p, i64p], C.c_int),
         "pxg_sys_destroy": ([vp], C.c_int),
         "pxg_sys_get_pattern": ([vp, vp, vp], C.c_int),
         "pxg_sys_pattern_device": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int),
+        "pxg_sys_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_sys_set_bc": ([vp, C.c_int, vp, vp, i64, C.c_double], C.c_int),
         "pxg_sys_assemble": ([vp, C.c_int, C.c_int, vp, vp, C.c_int, vp, vp, C.c_uint, vp], C.c_int),
         "pxg_build_facets": ([vp, i64p], C.c_int),
@@ -127,6 +133,7 @@ def load(path: str = LIB_PATH):
         "pxg_autotune": ([vp, C.POINTER(LhsOp), C.POINTER(LhsOp), C.POINTER(RhsOp), C.POINTER(TuneReport)], C.c_int),
         "pxg_close_matrix": ([vp, vp, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_interpolate": ([vp, C.c_int, C.c_double, vp, vp], C.c_int),
+        "pxg_get_qpoints": ([vp, vp, C.c_int, vp], C.c_int),
         "pxg_prune_csr_noalloc": ([vp, vp, vp, i64, vp, vp, vp, i64p, vp], C.c_int),
         "pxg_cg": ([vp, vp, vp, vp, i64, vp, vp, C.c_double, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), vp],
                    C.c_int),
@@ -147,6 +154,16 @@ def load(path: str = LIB_PATH):
         f.restype = res
     _lib = L
     return L
+
+
+def fp64_rate(device=0):
+    """(FP64 FMAs per second, ms of the timed launch) measured on a device."""
+    L = load()
+    r, ms = C.c_double(), C.c_double()
+    st = L.pxg_fp64_rate(int(device), C.byref(r), C.byref(ms))
+    if st:
+        raise PxgError(st, "fp64_rate")
+    return r.value, ms.value
 
 
 def _ptr(a):
@@ -322,6 +339,10 @@ class Context:
     def set_scatter(self, scatter, threads=0):
         self._check(self.L.pxg_set_scatter(self.h, int(scatter), int(threads)), "set_scatter")
 
+    def set_arithmetic(self, arith):
+        """ARITH_FP64 (default) or ARITH_DFL for this context's element kernels."""
+        self._check(self.L.pxg_set_arithmetic(self.h, int(arith)), "set_arithmetic")
+
     def colouring(self, with_order=False):
         """(number of colour classes, element order or None, class offsets or None)"""
         n = C.c_int()
@@ -351,6 +372,15 @@ class Context:
 
     def interpolate(self, fn, coef, v, stream=None):
         self._check(self.L.pxg_interpolate(self.h, int(fn), float(coef), _ptr(v), stream), "interpolate")
+
+    def get_qpoints(self, out=None, stream=None):
+        """CurFE::qpoint of every element and quadrature point: (nelem, nq, 3), into a
+        host array (default) or a device tensor `out`."""
+        nq = {P1TET: 4, P2TET: 11, Q1HEX: 8, Q2HEX: 27}[self.etype]
+        if out is None:
+            out = np.empty((self.nelem, nq, 3))
+        self._check(self.L.pxg_get_qpoints(self.h, _ptr(out), _mem(out), stream), "get_qpoints")
+        return out
 
     # --- solve and adjoint
     def cg(self, rp, ci, vals, b, x, rtol=1e-10, max_iter=10000, stream=None):
@@ -420,6 +450,13 @@ class System:
         rp, ci = C.c_void_p(), C.c_void_p()
         self._check(self.L.pxg_sys_pattern_device(self.h, C.byref(rp), C.byref(ci)), "sys_pattern_device")
         return rp.value, ci.value
+
+    def close_matrix(self, vals, rp, ci, vout, stream=None):
+        """closeMatrix on the system's pattern into device tensors; returns the kept count."""
+        n = C.c_int64()
+        self._check(self.L.pxg_sys_close_matrix(self.h, _ptr(vals), _ptr(rp), _ptr(ci), _ptr(vout), C.byref(n),
+                                                stream), "sys_close_matrix")
+        return n.value
 
     def set_bc(self, space, dofs, vals, diag=1.0):
         dofs = np.ascontiguousarray(dofs, dtype=np.uint32)

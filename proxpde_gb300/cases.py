@@ -15,7 +15,8 @@ Cases (seeded synthetic inputs, the generators of proxpde_gb300.meshgen):
 
 Each warm-up and timed repetition is one engine call; the line printed is JSON with the
 median event time of the repetitions.  The kernels' own names are in the output
-(`kernel`), for `ncu -k regex:<name>`.
+(`kernel`), for `ncu -k regex:<name>`.  --arith dfl runs the opt-in double-float
+kernels instead of the FP64 ones.
 """
 from __future__ import annotations
 
@@ -31,11 +32,12 @@ from . import meshgen
 SEED = 20261211
 
 ASSEMBLY = {
-    # case: element type, mesh generator, perturbation, k_e sigma, mass, rhs function, kernel
-    "q1hex": (L.Q1HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssembleQ1Group"),
-    "p2tet": (L.P2TET, meshgen.cube_tet6, 0.15, 0.5, True, L.FN_CONST, "kAssembleTet"),
-    "p1tet": (L.P1TET, meshgen.cube_tet6, 0.0, None, False, L.FN_CONST, "kAssembleTet"),
-    "q2hex": (L.Q2HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssembleQ2"),
+    # case: element type, mesh generator, perturbation, k_e sigma, mass, rhs function,
+    # kernel (FP64), kernel (double-float)
+    "q1hex": (L.Q1HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssembleQ1F64", "kAssembleQ1Group"),
+    "p2tet": (L.P2TET, meshgen.cube_tet6, 0.15, 0.5, True, L.FN_CONST, "kAssembleTet64", "kAssembleTet"),
+    "p1tet": (L.P1TET, meshgen.cube_tet6, 0.0, None, False, L.FN_CONST, "kAssembleTet64", "kAssembleTet"),
+    "q2hex": (L.Q2HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssemble", "kAssembleQ2"),
 }
 
 
@@ -56,14 +58,17 @@ def _events(fn, warmup, reps):
     return statistics.median(ts)
 
 
-def run_assembly(case, n, warmup, reps):
+def run_assembly(case, n, warmup, reps, arith="fp64"):
     import torch
 
-    t, gen, alpha, sigma, mass, fn, kernel = ASSEMBLY[case]
+    t, gen, alpha, sigma, mass, fn, k64, kdfl = ASSEMBLY[case]
+    kernel = k64 if arith == "fp64" else kdfl
     xyz, conn = gen(n)
     if alpha:
         xyz = meshgen.perturb(xyz, n, alpha, SEED)
     ctx = L.Context(0)
+    if arith == "dfl":
+        ctx.set_arithmetic(L.ARITH_DFL)
     ctx.set_mesh(t, xyz, conn)
     ndof = ctx.build_dofmap()
     nnz = ctx.build_pattern()
@@ -77,8 +82,8 @@ def run_assembly(case, n, warmup, reps):
     kw = dict(op0=opK, vals0=K, op1={"mass": 1, "mass_coef": 1.0} if mass else None, vals1=M,
               rhs={"kind": 1, "fn": fn, "coef": 1.0}, b=b)
     ms = _events(lambda: ctx.assemble(**kw), warmup, reps)
-    return {"case": case, "n": n, "elements": int(conn.shape[0]), "ndof": int(ndof), "nnz": int(nnz), "ms": ms,
-            "kernel": kernel, "includes": "memset of the outputs + element kernel"}
+    return {"case": case, "n": n, "arith": arith, "elements": int(conn.shape[0]), "ndof": int(ndof), "nnz": int(nnz),
+            "ms": ms, "kernel": kernel, "includes": "memset of the outputs + element kernel"}
 
 
 def run_batch(n, warmup, reps):
@@ -98,11 +103,12 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=32, help="cube size (batch: problems per element type)")
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--arith", choices=["fp64", "dfl"], default="fp64")
     a = ap.parse_args(argv)
     if a.case == "batch":
         out = run_batch(a.n, a.warmup, a.reps)
     else:
-        out = run_assembly(a.case, a.n, a.warmup, a.reps)
+        out = run_assembly(a.case, a.n, a.warmup, a.reps, a.arith)
     print(json.dumps(out))
 
 

@@ -119,16 +119,15 @@ pxg_status pxg_create(pxg_ctx ** out, int device)
     return PXG_ERR_NO_DEVICE;
   auto * c = new pxg_ctx;
   c->device = device;
-  char const * gen = getenv("PXG_Q1_GENERIC");
-  c->q1Generic = gen && gen[0] == '1';
-  char const * f64 = getenv("PXG_Q1_FP64");
-  c->q1Fp64 = f64 && f64[0] == '1';
-  char const * tf64 = getenv("PXG_TET_FP64");
-  c->tetFp64 = tf64 && tf64[0] == '1';
-  char const * q2f64 = getenv("PXG_Q2_FP64");
-  c->q2Fp64 = q2f64 && q2f64[0] == '1';
-  char const * thr = getenv("PXG_Q1_THREAD");
-  c->q1Thread = thr && thr[0] == '1';
+  auto envOn = [](char const * name) {
+    char const * v = getenv(name);
+    return v && v[0] == '1';
+  };
+  c->q1Generic = envOn("PXG_Q1_GENERIC");
+  c->q1Thread = envOn("PXG_Q1_THREAD");
+  c->q1Group = envOn("PXG_Q1_GROUP");
+  c->tetGeneric = envOn("PXG_TET_GENERIC");
+  c->q2Generic = envOn("PXG_Q2_GENERIC");
   pxg_status s = ensureDevice(c);
   if (s == PXG_OK && cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
     s = cudaFail(c, cudaGetLastError(), "SM count");
@@ -161,6 +160,13 @@ pxg_status pxg_destroy(pxg_ctx * ctx)
 pxg_status pxg_set_mesh(pxg_ctx * c, int etype, double const * xyz, int64_t nnodes,
                         uint32_t const * conn, int64_t nelem, int mem)
 {
+  if (c)
+  {
+    ++c->meshVer;
+    c->recipes.clear();
+    c->dofElemPtr.reset();
+    c->dofElem.reset();
+  }
   if (!c)
     return PXG_ERR_INVALID_ARG;
   if (etype < PXG_P1TET || etype > PXG_Q2HEX)
@@ -228,6 +234,10 @@ pxg_status pxg_set_mesh(pxg_ctx * c, int etype, double const * xyz, int64_t nnod
 
 pxg_status pxg_set_coords(pxg_ctx * c, double const * xyz, int mem, void * stream)
 {
+  if (c)
+  {
+    ++c->meshVer;
+  }
   if (!c || !xyz)
     return PXG_ERR_INVALID_ARG;
   if (c->etype < 0)
@@ -246,6 +256,13 @@ pxg_status pxg_set_coords(pxg_ctx * c, double const * xyz, int mem, void * strea
 
 pxg_status pxg_build_dofmap(pxg_ctx * c, int64_t * ndof)
 {
+  if (c)
+  {
+    ++c->meshVer;
+    c->recipes.clear();
+    c->dofElemPtr.reset();
+    c->dofElem.reset();
+  }
   if (!c)
     return PXG_ERR_INVALID_ARG;
   if (c->etype < 0)
@@ -266,6 +283,13 @@ pxg_status pxg_build_dofmap(pxg_ctx * c, int64_t * ndof)
 
 pxg_status pxg_set_dofmap(pxg_ctx * c, uint32_t const * em, int64_t ndof, int mem)
 {
+  if (c)
+  {
+    ++c->meshVer;
+    c->recipes.clear();
+    c->dofElemPtr.reset();
+    c->dofElem.reset();
+  }
   if (!c || !em || ndof <= 0)
     return PXG_ERR_INVALID_ARG;
   if (c->etype < 0)
@@ -355,6 +379,10 @@ pxg_status pxg_pattern_device(pxg_ctx * c, int32_t const ** rp, int32_t const **
 
 pxg_status pxg_set_coef(pxg_ctx * c, double const * k, int mem, void * stream)
 {
+  if (c)
+  {
+    ++c->coefVer;
+  }
   if (!c || !k)
     return PXG_ERR_INVALID_ARG;
   if (c->etype < 0)
@@ -377,6 +405,10 @@ pxg_status pxg_set_coef(pxg_ctx * c, double const * k, int mem, void * stream)
 pxg_status pxg_set_bc(pxg_ctx * c, uint32_t const * dofs, double const * vals, int64_t n,
                       double diag, int mem)
 {
+  if (c)
+  {
+    ++c->bcVer;
+  }
   if (!c || n < 0 || (n > 0 && (!dofs || !vals)))
     return PXG_ERR_INVALID_ARG;
   if (c->ndof <= 0)

@@ -37,6 +37,7 @@ __constant__ double cQ2phi[27 * 27], cQ2dphi[27 * 27 * 3], cQ2w[27], cQ2xi[27 * 
 // the affine elements' reference tensors as hi/lo float pairs (kAssembleTet)
 __constant__ float2 cP1Td[6 * 16], cP1Md[16], cP2Td[6 * 100], cP2Md[100];
 __constant__ double cP1I[4], cP2I[10]; // sum_q w_q phi_i(q): the load vector of f = 1
+__constant__ double cP1Ws;             // sum_q w_q of the Tet4 rule (the reference volume)
 
 template <int T>
 __device__ __forceinline__ double PHI(int q, int i)
@@ -281,6 +282,10 @@ pxg_status initTables(pxg_ctx * c)
         PXG_CUDA(c, cudaMemcpyToSymbol(cP1Td, Td.data(), Td.size() * sizeof(float2)));
         PXG_CUDA(c, cudaMemcpyToSymbol(cP1Md, Md.data(), Md.size() * sizeof(float2)));
         PXG_CUDA(c, cudaMemcpyToSymbol(cP1I, I.data(), I.size() * 8));
+        double ws = 0.;
+        for (int q = 0; q < nq; ++q)
+          ws += w[q];
+        PXG_CUDA(c, cudaMemcpyToSymbol(cP1Ws, &ws, 8));
       }
       else
       {
@@ -461,6 +466,13 @@ __global__ void __launch_bounds__(NT) kAssemble(AsmArgs a)
         fq[q] = evalFn(a.fn, a.rc, xq[0], xq[1], xq[2]);
       }
     }
+  }
+  if (a.rkind == 3)
+  {
+    // values of f at the quadrature points, evaluated by the caller (pxg_get_qpoints)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      fq[q] = a.rc * a.field[e * NQ + q];
   }
   if (a.rkind == 2)
   {
@@ -971,6 +983,525 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
   }
 }
 
+// ------------------------------------------------- tetrahedra in FP64 arithmetic
+// kAssembleTet64 (the default for P1/P2): the reference-tensor form of kAssembleTet in
+// IEEE binary64 throughout.  Per element: J from the vertex differences, adj(J),
+// |det J|, G = adj adj^T / |det J| (with a single stiffness operator's coefficient
+// folded in); an entry is the six-term product of G with the reference tensor (FP64
+// constant memory), the mass entry |det J| Mhat_ij (a single mass operator's
+// coefficient folded into |det J|).  About 450 FP64 operations per P2 element
+// against about 1,000 for the per-quadrature-point form of kAssemble.
+template <int T, int NT>
+__global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
+{
+  constexpr int N = Elem<T>::N, NQ = Elem<T>::NQ;
+  int64_t const i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i0 >= a.nelem)
+    return;
+  int64_t const e = elemOf(a, i0);
+
+  double X[4][3];
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+  {
+    uint32_t const id = a.conn[e * 4 + v];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      X[v][d] = a.xyz[3 * (int64_t)id + d];
+  }
+  uint32_t dof[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    dof[i] = a.emap[e * N + i];
+  uint32_t cons = 0;
+  if (a.bcMask)
+  {
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (a.bcMask[dof[i]])
+        cons |= 1u << i;
+  }
+  LhsDev const & op0 = a.op[0];
+  LhsDev const & op1 = a.op[1];
+  bool const k0 = op0.on && op0.stiff, k1 = op1.on && op1.stiff;
+  bool const m0 = op0.on && op0.mass, m1 = op1.on && op1.mass;
+  bool const needK = k0 || k1, needM = m0 || m1;
+  bool const kE = usesCoef(op0) || usesCoef(op1);
+  double const kfac = (kE && a.kE) ? a.kE[e] : 1.0;
+
+  double J[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc)
+      J[r][cc] = X[cc + 1][r] - X[0][r];
+  double A[3][3];
+  double const adet = fabs(adj3(J, A));
+  bool const foldK = k0 != k1, foldM = m0 != m1;
+  double const ks0 = k0 ? (op0.stiff == 2 ? op0.sc * kfac : op0.sc) : 0.;
+  double const ks1 = k1 ? (op1.stiff == 2 ? op1.sc * kfac : op1.sc) : 0.;
+  double const ms0 = m0 ? massCoef(op0, kfac) : 0., ms1 = m1 ? massCoef(op1, kfac) : 0.;
+  // 1/|det J|: hardware estimate and one third-order Newton step (y (1 + e + e^2),
+  // e = 1 - x y), instead of a full-precision division with its special cases
+  double ra;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(ra) : "d"(adet));
+  {
+    double const e = fma(-adet, ra, 1.0);
+    ra = fma(ra, fma(e, e, e), ra);
+  }
+  double G[6];
+  gram(A, (foldK ? (k0 ? ks0 : ks1) : 1.0) * (T == P1TET ? ra * cP1Ws : ra), G);
+  double const am = foldM ? (m0 ? ms0 : ms1) * adet : adet;
+  // P1: grad phi_i |det J| are the adjugate rows (i = 1..3) and minus their sum (i = 0),
+  // so K_ij = k / (6 |det J|) A_i . A_j reads the Gram entries of the adjugate directly:
+  // K_(a+1)(b+1) = G_ab, K_0(b+1) = -sum_a G_ab, K_00 = sum_ab G_ab, with G carrying
+  // the sum of the Tet4 weights (the reference volume 1/6)
+  double K1[4][4];
+  if constexpr (T == P1TET)
+  {
+    double const Gs[3][3] = {{G[0], G[3], G[4]}, {G[3], G[1], G[5]}, {G[4], G[5], G[2]}};
+    double cs[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+    {
+      cs[b] = Gs[0][b] + (Gs[1][b] + Gs[2][b]);
+      K1[0][b + 1] = -cs[b];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        K1[a + 1][b + 1] = Gs[a][b];
+    }
+    K1[0][0] = cs[0] + (cs[1] + cs[2]);
+  }
+
+  int32_t rpn[N];
+#pragma unroll
+  for (int n = 0; n < N; ++n)
+    rpn[n] = a.rowPtr[dof[n]];
+  bool const anyBc = cons && ((op0.on && op0.bc) || (op1.on && op1.bc));
+  uint16_t const * rk = a.rank + e * (int64_t)(N * N);
+  constexpr int kRowUnroll = N <= 4 ? N : 1;
+  bool const kmPair = op0.on && op0.stiff && !op0.mass && op1.on && !op1.stiff && op1.mass;
+  // the usual operator pair (stiffness-only, then mass-only, both folded) in a warp
+  // without constrained entries: a loop without per-entry operator branches
+  bool const fast = kmPair && !__any_sync(__activemask(), anyBc);
+#pragma unroll kRowUnroll
+  for (int i = 0; i < N; ++i)
+  {
+    uint32_t const dofi = pickN(dof, i);
+    int32_t const rpi = pickN(rpn, i);
+    bool const ci = (cons >> i) & 1u;
+#pragma unroll kRowUnroll
+    for (int j = i; j < N; ++j)
+    {
+      double kv = 0., mv = 0.;
+      if (needK)
+      {
+        if constexpr (T == P1TET)
+          kv = K1[i][j];
+        else
+        {
+          kv = G[0] * TT<T>(0, i, j);
+#pragma unroll
+          for (int k = 1; k < 6; ++k)
+            kv = fma(G[k], TT<T>(k, i, j), kv);
+        }
+      }
+      if (needM)
+        mv = am * MHAT<T>(i, j);
+      int32_t const pij = rpi + rk[i * N + j];
+      int32_t const pji = pickN(rpn, j) + rk[j * N + i];
+      if (fast)
+      {
+        red(op0.vals + pij, kv);
+        red(op1.vals + pij, mv);
+        if (j != i)
+        {
+          red(op0.vals + pji, kv);
+          red(op1.vals + pji, mv);
+        }
+        continue;
+      }
+      bool const cj = (cons >> j) & 1u;
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+      {
+        LhsDev const & op = a.op[m];
+        if (!op.on)
+          continue;
+        double v;
+        if (op.stiff)
+        {
+          v = foldK ? kv : (m ? ks1 : ks0) * kv;
+          if (op.mass)
+            v = foldM ? v + mv : fma(m ? ms1 : ms0, mv, v);
+        }
+        else
+          v = foldM ? mv : (m ? ms1 : ms0) * mv;
+        if (anyBc && op.bc && (ci || cj))
+        {
+          condenseTet(op.vals + pij, a.bcDiag, a.b, dofi, pickN(dof, j), a.bcVal, ci, cj, i == j, v);
+          continue;
+        }
+        red(op.vals + pij, v);
+        if (j != i)
+          red(op.vals + pji, v);
+      }
+    }
+  }
+  if (!a.b)
+    return;
+  if (anyBc)
+  {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+    {
+      if (!a.op[m].on || !a.op[m].bc)
+        continue;
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+        if ((cons >> n) & 1u)
+        {
+          double const h = a.bcVal[dof[n]];
+          if (h != 0.)
+            red(a.b + dof[n], h);
+        }
+    }
+  }
+  if (!a.rkind)
+    return;
+  if (a.rkind == 1 && a.fn == PXG_FN_CONST)
+  {
+    double const f = evalFn(a.fn, a.rc, 0., 0., 0.) * adet;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (!(a.rbc && ((cons >> i) & 1u)))
+        red(a.b + dof[i], f * PINT<T>(i));
+    return;
+  }
+  double fq[NQ];
+  if (a.rkind == 1)
+  {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double xq[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        xq[r] = X[0][r] + (J[r][0] * XI<T>(q, 0) + J[r][1] * XI<T>(q, 1) + J[r][2] * XI<T>(q, 2));
+      fq[q] = evalFn(a.fn, a.rc, xq[0], xq[1], xq[2]);
+    }
+  }
+  else
+  {
+    double loc[N];
+#pragma unroll
+    for (int n = 0; n < N; ++n)
+      loc[n] = a.field[dof[n]];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+    {
+      double s = 0.;
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+        s += PHI<T>(q, n) * loc[n];
+      fq[q] = a.rc * s;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+  {
+    if (a.rbc && ((cons >> i) & 1u))
+      continue;
+    double fe = 0.;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+      fe += (adet * WQ<T>(q)) * PHI<T>(q, i) * fq[q];
+    red(a.b + dof[i], fe);
+  }
+}
+
+// CurFE::qpoint (include/curfe.hpp:80) of every element and quadrature point:
+// origin + J(xi_q) xi_q, J from the mapping points as in kAssemble; origin = the first
+// vertex (tetrahedra, include/geo.hpp:583-588) or the vertex average (hexahedra,
+// geo.hpp:721-728).  One thread per element; out[(e * NQ + q) * 3 + d].
+template <int T>
+__global__ void __launch_bounds__(128) kQpoints(int64_t nelem, double const * __restrict__ xyz,
+                                                uint32_t const * __restrict__ conn, double * __restrict__ out)
+{
+  constexpr int NV = Elem<T>::NV, N = Elem<T>::N, NQ = Elem<T>::NQ;
+  int64_t const e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= nelem)
+    return;
+  double X[NV][3];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    uint32_t const id = conn[e * NV + v];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      X[v][d] = xyz[3 * (int64_t)id + d];
+  }
+  double * o = out + e * NQ * 3;
+  if constexpr (!Elem<T>::hex)
+  {
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        o[3 * q + r] = X[0][r] + ((X[1][r] - X[0][r]) * XI<T>(q, 0) + (X[2][r] - X[0][r]) * XI<T>(q, 1) +
+                                  (X[3][r] - X[0][r]) * XI<T>(q, 2));
+  }
+  else
+  {
+    double P[N][3];
+    mappingPoints<T>(X, P);
+    double org[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      org[d] = .125 * (X[0][d] + X[1][d] + X[2][d] + X[3][d] + X[4][d] + X[5][d] + X[6][d] + X[7][d]);
+#pragma unroll 1
+    for (int q = 0; q < NQ; ++q)
+    {
+      double J[3][3] = {{0., 0., 0.}, {0., 0., 0.}, {0., 0., 0.}};
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc)
+            J[r][cc] += P[n][r] * DPHI<T>(q, n, cc);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        o[3 * q + r] = org[r] + (J[r][0] * XI<T>(q, 0) + J[r][1] * XI<T>(q, 1) + J[r][2] * XI<T>(q, 2));
+    }
+  }
+}
+
+// ------------------------------------------- near-zero entries in the reference order
+// closeMatrix's prune(1., 1e-16) (include/builder.hpp:369) decides on absolute values,
+// so an entry that is mathematically zero is kept or dropped by the round-off of its
+// evaluation: on a jittered P2 mesh the reference's CurFE form leaves 1e-16 residues
+// where the engine's reference-tensor form gives exact zeros.  For the entries whose
+// value lies within the engine's round-off of the threshold (|v| <= 1e-16 + 64 eps
+// max|row|), the value is recomputed in the reference's evaluation order: per element,
+// CurFE::reinit (include/curfe.hpp:50-103: J from the mapping points, J^T J, its
+// cofactor inverse, sqrt(det), J^+, dphi = dphiRef J^+) and the stiffness / mass sums
+// over the quadrature points (include/assembly_lhs.hpp:52-65, 207-221) with the
+// Dirichlet condensation of builder.hpp:76-124; over elements, the triplets' sum in
+// emission order (setFromTriplets: the first contribution, then each later one added).
+// Every operation is a separately rounded IEEE operation (the intrinsics below are
+// never contracted into FMAs), in the order the reference's expressions give.
+__device__ __forceinline__ double dA(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dS(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dM(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dD(double a, double b) { return __ddiv_rn(a, b); }
+
+struct RefOp
+{
+  int stiff, mass, bc;
+  double sc, mc;
+};
+struct RepairArgs
+{
+  double const * xyz;
+  uint32_t const * conn;
+  uint32_t const * emap;
+  int32_t const * rowPtr;
+  int32_t const * colIdx;
+  double const * kE;
+  uint8_t const * bcMask;
+  double bcDiag;
+  int32_t const * dofElemPtr;
+  uint32_t const * dofElem;
+  RefOp ops[8];
+  int nops;
+  int64_t const * flagged; // positions in the structural pattern
+  int32_t const * flaggedRow;
+  int64_t nflagged;
+  double * vals; // values on the structural pattern, the flagged ones overwritten
+};
+
+// the element's local entry (i, j) of one operator, before any condensation
+template <int T>
+__device__ double refElemEntry(RepairArgs const & a, int64_t e, int i, int j, RefOp const & op)
+{
+  constexpr int NV = Elem<T>::NV, N = Elem<T>::N, NQ = Elem<T>::NQ;
+  double X[NV][3];
+  for (int v = 0; v < NV; ++v)
+  {
+    uint32_t const id = a.conn[e * NV + v];
+    for (int d = 0; d < 3; ++d)
+      X[v][d] = a.xyz[3 * (int64_t)id + d];
+  }
+  double P[N][3];
+  mappingPoints<T>(X, P);
+  double const kfac = a.kE ? a.kE[e] : 1.0;
+  double jxw[NQ], Di[NQ][3], Dj[NQ][3];
+  for (int q = 0; q < NQ; ++q)
+  {
+    double J[3][3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c)
+        J[r][c] = 0.;
+    for (int n = 0; n < N; ++n)
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+          J[r][c] = dA(J[r][c], dM(P[n][r], DPHI<T>(q, n, c)));
+    double A[3][3];
+    for (int x = 0; x < 3; ++x)
+      for (int y = 0; y < 3; ++y)
+        A[x][y] = dA(dA(dM(J[0][x], J[0][y]), dM(J[1][x], J[1][y])), dM(J[2][x], J[2][y]));
+    double const c00 = dS(dM(A[1][1], A[2][2]), dM(A[1][2], A[2][1]));
+    double const c01 = dS(dM(A[1][2], A[2][0]), dM(A[1][0], A[2][2]));
+    double const c02 = dS(dM(A[1][0], A[2][1]), dM(A[1][1], A[2][0]));
+    double const det = dA(dA(dM(A[0][0], c00), dM(A[0][1], c01)), dM(A[0][2], c02));
+    double Ai[3][3];
+    Ai[0][0] = dD(c00, det);
+    Ai[1][0] = dD(c01, det);
+    Ai[2][0] = dD(c02, det);
+    Ai[0][1] = dD(dS(dM(A[0][2], A[2][1]), dM(A[0][1], A[2][2])), det);
+    Ai[1][1] = dD(dS(dM(A[0][0], A[2][2]), dM(A[0][2], A[2][0])), det);
+    Ai[2][1] = dD(dS(dM(A[0][1], A[2][0]), dM(A[0][0], A[2][1])), det);
+    Ai[0][2] = dD(dS(dM(A[0][1], A[1][2]), dM(A[0][2], A[1][1])), det);
+    Ai[1][2] = dD(dS(dM(A[0][2], A[1][0]), dM(A[0][0], A[1][2])), det);
+    Ai[2][2] = dD(dS(dM(A[0][0], A[1][1]), dM(A[0][1], A[1][0])), det);
+    double Jp[3][3];
+    for (int x = 0; x < 3; ++x)
+      for (int c = 0; c < 3; ++c)
+        Jp[x][c] = dA(dA(dM(Ai[x][0], J[c][0]), dM(Ai[x][1], J[c][1])), dM(Ai[x][2], J[c][2]));
+    jxw[q] = dM(__dsqrt_rn(det), WQ<T>(q));
+    for (int c = 0; c < 3; ++c)
+    {
+      Di[q][c] = dA(dA(dM(DPHI<T>(q, i, 0), Jp[0][c]), dM(DPHI<T>(q, i, 1), Jp[1][c])), dM(DPHI<T>(q, i, 2), Jp[2][c]));
+      Dj[q][c] = dA(dA(dM(DPHI<T>(q, j, 0), Jp[0][c]), dM(DPHI<T>(q, j, 1), Jp[1][c])), dM(DPHI<T>(q, j, 2), Jp[2][c]));
+    }
+  }
+  double ke = 0.;
+  if (op.stiff)
+  {
+    double const c = op.stiff == 1 ? op.sc : dM(1.0, dM(op.sc, kfac));
+    for (int q = 0; q < NQ; ++q)
+    {
+      double const sq = dM(c, jxw[q]);
+      double const a0 = dM(sq, Di[q][0]), a1 = dM(sq, Di[q][1]), a2 = dM(sq, Di[q][2]);
+      ke = dA(ke, dA(dA(dM(a0, Dj[q][0]), dM(a1, Dj[q][1])), dM(a2, Dj[q][2])));
+    }
+  }
+  if (op.mass)
+  {
+    double const c = op.mass == 1 ? op.mc : dM(1.0, dM(op.mc, kfac));
+    for (int q = 0; q < NQ; ++q)
+    {
+      double const sq = dM(c, jxw[q]);
+      ke = dA(ke, dM(dM(sq, PHI<T>(q, i)), PHI<T>(q, j)));
+    }
+  }
+  return ke;
+}
+
+// one thread per flagged entry: the sum of the element contributions in emission order
+// (operators in call order, elements in ascending order)
+template <int T>
+__global__ void __launch_bounds__(128) kRepairEntries(RepairArgs a)
+{
+  constexpr int N = Elem<T>::N;
+  int64_t const k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= a.nflagged)
+    return;
+  int64_t const p = a.flagged[k];
+  int32_t const r = a.flaggedRow[k];
+  int32_t const col = a.colIdx[p];
+  bool const consR = a.bcMask && a.bcMask[r], consC = a.bcMask && a.bcMask[col];
+  double v = 0.;
+  bool first = true;
+  for (int o = 0; o < a.nops; ++o)
+  {
+    RefOp const op = a.ops[o];
+    for (int32_t t = a.dofElemPtr[r]; t < a.dofElemPtr[r + 1]; ++t)
+    {
+      int64_t const e = a.dofElem[t];
+      int i = -1, j = -1;
+      for (int n = 0; n < N; ++n)
+      {
+        uint32_t const d = a.emap[e * N + n];
+        if ((int32_t)d == r)
+          i = n;
+        if ((int32_t)d == col)
+          j = n;
+      }
+      if (i < 0 || j < 0)
+        continue;
+      double ke;
+      if (op.bc && (consR || consC))
+        ke = (r == col && consR) ? a.bcDiag : 0.;
+      else
+        ke = refElemEntry<T>(a, e, i, j, op);
+      v = first ? ke : dA(v, ke);
+      first = false;
+    }
+  }
+  a.vals[p] = v;
+}
+
+// entries within the engine's round-off of the prune threshold: |v| <= 1e-16 +
+// 64 eps max|row|.  count != nullptr: count them; else write their positions and rows
+__global__ void kFlagNearZero(int32_t const * __restrict__ rowPtr, double const * __restrict__ vals, int64_t n,
+                              unsigned long long * count, int64_t * pos, int32_t * row, int64_t cap)
+{
+  int64_t const r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n)
+    return;
+  double mx = 0.;
+  for (int32_t p = rowPtr[r]; p < rowPtr[r + 1]; ++p)
+    mx = fmax(mx, fabs(vals[p]));
+  double const tau = 1e-16 + 64. * 2.220446049250313e-16 * mx;
+  for (int32_t p = rowPtr[r]; p < rowPtr[r + 1]; ++p)
+    if (fabs(vals[p]) <= tau)
+    {
+      unsigned long long const k = atomicAdd(count, 1ull);
+      if (pos && (int64_t)k < cap)
+      {
+        pos[k] = p;
+        row[k] = (int32_t)r;
+      }
+    }
+}
+
+// element lists per DOF: counts, then the fill, then each list sorted ascending
+__global__ void kDofElemCount(uint32_t const * __restrict__ emap, int64_t nelem, int N, int32_t * cnt)
+{
+  int64_t const t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nelem * N)
+    return;
+  atomicAdd(cnt + emap[t], 1);
+}
+__global__ void kDofElemFill(uint32_t const * __restrict__ emap, int64_t nelem, int N, int32_t * cursor,
+                             uint32_t * list)
+{
+  int64_t const t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nelem * N)
+    return;
+  int32_t const at = atomicAdd(cursor + emap[t], 1);
+  list[at] = (uint32_t)(t / N);
+}
+__global__ void kDofElemSort(int32_t const * __restrict__ ptr, int64_t ndof, uint32_t * list)
+{
+  int64_t const d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (d >= ndof)
+    return;
+  for (int32_t a = ptr[d] + 1; a < ptr[d + 1]; ++a)
+  {
+    uint32_t const v = list[a];
+    int32_t b = a - 1;
+    while (b >= ptr[d] && list[b] > v)
+    {
+      list[b + 1] = list[b];
+      --b;
+    }
+    list[b + 1] = v;
+  }
+}
+
 template <int T>
 __global__ void kInterpolate(int64_t nelem, double const * __restrict__ xyz, uint32_t const * __restrict__ conn,
                              uint32_t const * __restrict__ emap, int fn, double c, double * __restrict__ v)
@@ -1199,7 +1730,7 @@ pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, 
     if (c->q1Generic)
       kAdjointGrad<Q1HEX><<<blocks, 128, 0, s>>>(a);
     else
-      launchAdjointGradQ1(a, s, c->q1Fp64);
+      launchAdjointGradQ1(a, s, c->arith == PXG_ARITH_FP64);
     break;
   case Q2HEX:
     kAdjointGrad<Q2HEX><<<blocks, 128, 0, s>>>(a);
@@ -1232,6 +1763,20 @@ void launchAssembleTet(AsmArgs const & a, cudaStream_t s, int threads)
 }
 
 template <int T>
+void launchAssembleTet64(AsmArgs const & a, cudaStream_t s, int threads)
+{
+  auto go = [&](auto kern, int nt) {
+    unsigned const blocks = (unsigned)((a.nelem + nt - 1) / nt);
+    kern<<<blocks, nt, 0, s>>>(a);
+  };
+  if (threads == 64)
+    return go(kAssembleTet64<T, 64>, 64);
+  if (threads == 256)
+    return go(kAssembleTet64<T, 256>, 256);
+  go(kAssembleTet64<T, 128>, 128);
+}
+
+template <int T>
 void launchAssemble(AsmArgs const & a, cudaStream_t s, int threads)
 {
   auto go = [&](auto kern, int nt) {
@@ -1248,14 +1793,111 @@ void launchAssemble(AsmArgs const & a, cudaStream_t s, int threads)
   go(kAssemble<T, 128>, 128);
 }
 
+} // namespace
+
+// Remember what pxg_assemble adds into a value array (its recipe), for the
+// reference-order recomputation of its near-zero entries at pxg_close_matrix.
+void recordRecipe(pxg_ctx * c, double const * vals, pxg_lhs_op const & o, bool accumulate)
+{
+  auto & rs = c->recipes;
+  size_t k = 0;
+  while (k < rs.size() && rs[k].vals != vals)
+    ++k;
+  if (k == rs.size())
+  {
+    if (rs.size() >= 16)
+      rs.erase(rs.begin());
+    rs.push_back(pxg_ctx::Recipe{});
+    k = rs.size() - 1;
+    rs[k].vals = vals;
+  }
+  pxg_ctx::Recipe & R = rs[k];
+  if (!accumulate)
+  {
+    R.ops.clear();
+    R.valid = true;
+    R.meshVer = c->meshVer, R.coefVer = c->coefVer, R.bcVer = c->bcVer;
+  }
+  else if (R.meshVer != c->meshVer || R.coefVer != c->coefVer || R.bcVer != c->bcVer)
+    R.valid = false; // calls on different data: the sum cannot be recomputed
+  if (R.ops.size() >= 8)
+    R.valid = false;
+  else
+    R.ops.push_back(pxg_ctx::LhsRec{o.stiffness, o.mass, o.apply_bc, o.stiff_coef, o.mass_coef});
+}
+
+// the element lists of every DOF, ascending (built once per DOF map)
+pxg_status ensureDofElem(pxg_ctx * c)
+{
+  if (c->dofElemPtr.p)
+    return PXG_OK;
+  int64_t const n = c->ndof, m = c->nelem * c->N;
+  DevBuf<int32_t> cnt, cursor;
+  PXG_CUDA(c, cnt.alloc(n + 1));
+  PXG_CUDA(c, cudaMemset(cnt.p, 0, (n + 1) * 4));
+  unsigned const bm = (unsigned)((m + 255) / 256), bn = (unsigned)((n + 255) / 256);
+  kDofElemCount<<<bm, 256>>>(c->emap.p, c->nelem, c->N, cnt.p);
+  PXG_CUDA(c, c->dofElemPtr.alloc(n + 1));
+  size_t tb = 0;
+  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt.p, c->dofElemPtr.p, n + 1));
+  DevBuf<unsigned char> tmp;
+  PXG_CUDA(c, tmp.alloc(tb));
+  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, tb, cnt.p, c->dofElemPtr.p, n + 1));
+  PXG_CUDA(c, cursor.alloc(n + 1));
+  PXG_CUDA(c, cudaMemcpy(cursor.p, c->dofElemPtr.p, (n + 1) * 4, cudaMemcpyDeviceToDevice));
+  PXG_CUDA(c, c->dofElem.alloc(m));
+  kDofElemFill<<<bm, 256>>>(c->emap.p, c->nelem, c->N, cursor.p, c->dofElem.p);
+  kDofElemSort<<<bn, 256>>>(c->dofElemPtr.p, n, c->dofElem.p);
+  PXG_CUDA(c, cudaGetLastError());
+  PXG_CUDA(c, cudaDeviceSynchronize());
+  return PXG_OK;
+}
+
+// Builder::closeMatrix's prune(1., 1e-16) and compaction of a structural CSR (row
+// pointers rowPtr[n + 1], columns colIdx) with values vals: kept entries per row, their
+// exclusive scan (the new row pointers), the compaction, and the kept count read back
+// (the stream is synchronised).  Scratch is allocated per call on c's device.
+namespace pxg
+{
+pxg_status closeCsr(pxg_ctx * c, int32_t const * rowPtr, int32_t const * colIdx, int64_t n, double const * vals,
+                    int32_t * rp, int32_t * ci, double * vout, int64_t * nnzOut, cudaStream_t s)
+{
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  DevBuf<int32_t> kept;
+  PXG_CUDA(c, kept.alloc(n + 1));
+  unsigned const blocks = (unsigned)((n + 255) / 256);
+  kRowKept<<<blocks, 256, 0, s>>>(rowPtr, vals, n, kept.p);
+  PXG_CUDA(c, cudaMemsetAsync(kept.p + n, 0, 4, s));
+  size_t tb = 0;
+  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(nullptr, tb, kept.p, rp, n + 1, s));
+  DevBuf<unsigned char> tmp;
+  PXG_CUDA(c, tmp.alloc(tb));
+  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, tb, kept.p, rp, n + 1, s));
+  kCompact<<<blocks, 256, 0, s>>>(rowPtr, colIdx, vals, n, rp, ci, vout);
+  PXG_CUDA(c, cudaGetLastError());
+  int32_t tot = 0;
+  PXG_CUDA(c, cudaMemcpyAsync(&tot, rp + n, 4, cudaMemcpyDeviceToHost, s));
+  PXG_CUDA(c, cudaStreamSynchronize(s));
+  *nnzOut = tot;
+  return PXG_OK;
+}
+} // namespace pxg
+
+namespace
+{
 // Candidate thread counts of the autotuner for an element type (0-terminated)
 void threadCandidates(pxg_ctx const * c, int (&out)[4])
 {
   out[0] = out[1] = out[2] = out[3] = 0;
+  bool const fp64 = c->arith == PXG_ARITH_FP64;
   if (c->etype == P1TET || c->etype == P2TET)
     out[0] = 64, out[1] = 128, out[2] = 256;
-  else if (c->etype == Q1HEX && !c->q1Generic && !c->q1Thread)
+  else if (c->etype == Q1HEX && !c->q1Generic && !c->q1Thread && (c->q1Group || !fp64))
     out[0] = 256, out[1] = 512;
+  else if (c->etype == Q1HEX && !c->q1Generic && !c->q1Thread)
+    out[0] = 64, out[1] = 128;
   else
     out[0] = 128;
 }
@@ -1302,8 +1944,10 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
   }
   if (rhs && rhs->kind)
   {
-    if (rhs->kind < 0 || rhs->kind > 2)
+    if (rhs->kind < 0 || rhs->kind > 3)
       return fail(c, PXG_ERR_INVALID_ARG, "rhs kind %d", rhs->kind);
+    if (rhs->kind == 3 && !rhs->field)
+      return fail(c, PXG_ERR_INVALID_ARG, "rhs kind 3 needs the values at the quadrature points");
     if (rhs->kind == 1 && (rhs->fn < 0 || rhs->fn > PXG_FN_COORD_Z))
       return fail(c, PXG_ERR_INVALID_ARG, "unknown analytic function %d", rhs->fn);
     if (rhs->kind == 2 && !rhs->field)
@@ -1323,6 +1967,9 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
   pxg_status st = ensureDevice(c);
   if (st != PXG_OK)
     return st;
+  for (int m = 0; m < 2; ++m)
+    if (a.op[m].on)
+      recordRecipe(c, outs[m], *ops[m], (flags & PXG_ACCUMULATE) != 0);
   if (!(flags & PXG_ACCUMULATE))
   {
     for (int m = 0; m < 2; ++m)
@@ -1331,34 +1978,75 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     if (b)
       PXG_CUDA(c, cudaMemsetAsync(b, 0, (size_t)c->ndof * 8, s));
   }
-  auto launch = [&](AsmArgs const & la) {
+  // rhs kind 3 (values at the quadrature points) runs in the per-quadrature-point FP64
+  // kernel, after the element kernel has done the matrices and their BC lifts
+  auto launchValuesLoad = [&](AsmArgs const & la) {
+    AsmArgs l2 = la;
+    l2.op[0].on = l2.op[1].on = 0;
     switch (c->etype)
     {
     case P1TET:
-      if (c->tetFp64)
+      launchAssemble<P1TET>(l2, s, 0);
+      break;
+    case P2TET:
+      launchAssemble<P2TET>(l2, s, 0);
+      break;
+    case Q1HEX:
+      launchAssemble<Q1HEX>(l2, s, 0);
+      break;
+    case Q2HEX:
+      launchAssemble<Q2HEX>(l2, s, 0);
+      break;
+    }
+  };
+  auto launchElem = [&](AsmArgs const & la) {
+    bool const fp64 = c->arith == PXG_ARITH_FP64;
+    switch (c->etype)
+    {
+    case P1TET:
+      if (c->tetGeneric)
         launchAssemble<P1TET>(la, s, c->threads);
+      else if (fp64)
+        launchAssembleTet64<P1TET>(la, s, c->threads);
       else
         launchAssembleTet<P1TET>(la, s, c->threads);
       break;
     case P2TET:
-      if (c->tetFp64)
+      if (c->tetGeneric)
         launchAssemble<P2TET>(la, s, c->threads);
+      else if (fp64)
+        launchAssembleTet64<P2TET>(la, s, c->threads);
       else
         launchAssembleTet<P2TET>(la, s, c->threads);
       break;
     case Q1HEX:
       if (c->q1Generic)
         launchAssemble<Q1HEX>(la, s, c->threads);
+      else if (c->q1Thread || c->q1Group || !fp64)
+        launchAssembleQ1(la, s, fp64, c->q1Thread, c->threads);
       else
-        launchAssembleQ1(la, s, c->q1Fp64, c->q1Thread, c->threads);
+        launchAssembleQ1F64(la, s, c->threads);
       break;
     case Q2HEX:
-      if (c->q2Fp64)
+      if (c->q2Generic)
         launchAssemble<Q2HEX>(la, s, c->threads);
+      else if (fp64)
+        launchAssembleQ2F64(la, s);
       else
         launchAssembleQ2(la, s, c->sms);
       break;
     }
+  };
+  auto launch = [&](AsmArgs const & la) {
+    if (la.rkind != 3)
+      return launchElem(la);
+    if (la.op[0].on || la.op[1].on)
+    {
+      AsmArgs l1 = la;
+      l1.rkind = 0;
+      launchElem(l1);
+    }
+    launchValuesLoad(la);
   };
   if (c->scatter == PXG_SCATTER_COLOUR)
   {
@@ -1411,6 +2099,17 @@ pxg_status pxg_set_scatter(pxg_ctx * c, int scatter, int threads)
     return st;
   c->scatter = scatter;
   c->threads = threads;
+  return PXG_OK;
+}
+
+pxg_status pxg_set_arithmetic(pxg_ctx * c, int arith)
+{
+  if (!c)
+    return PXG_ERR_INVALID_ARG;
+  if (arith != PXG_ARITH_FP64 && arith != PXG_ARITH_DFL)
+    return fail(c, PXG_ERR_INVALID_ARG, "arithmetic %d", arith);
+  c->arith = arith;
+  c->threads = 0;
   return PXG_OK;
 }
 
@@ -1559,23 +2258,112 @@ pxg_status pxg_close_matrix(pxg_ctx * c, double const * vals, int32_t * rp, int3
   if (st != PXG_OK)
     return st;
   cudaStream_t const s = (cudaStream_t)stream;
+  // an array this context assembled, on unchanged data: its near-zero entries are
+  // recomputed in the reference's evaluation order before the prune
+  pxg_ctx::Recipe const * R = nullptr;
+  for (auto const & r: c->recipes)
+    if (r.vals == vals && r.valid && r.meshVer == c->meshVer && r.coefVer == c->coefVer && r.bcVer == c->bcVer)
+      R = &r;
+  if (!R)
+    return closeCsr(c, c->rowPtr.p, c->colIdx.p, c->ndof, vals, rp, ci, vout, nnzOut, s);
   int64_t const n = c->ndof;
-  DevBuf<int32_t> kept;
-  PXG_CUDA(c, kept.alloc(n + 1));
-  unsigned const blocks = (unsigned)((n + 255) / 256);
-  kRowKept<<<blocks, 256, 0, s>>>(c->rowPtr.p, vals, n, kept.p);
-  PXG_CUDA(c, cudaMemsetAsync(kept.p + n, 0, 4, s));
-  size_t tb = 0;
-  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(nullptr, tb, kept.p, rp, n + 1, s));
-  DevBuf<unsigned char> tmp;
-  PXG_CUDA(c, tmp.alloc(tb));
-  PXG_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, tb, kept.p, rp, n + 1, s));
-  kCompact<<<blocks, 256, 0, s>>>(c->rowPtr.p, c->colIdx.p, vals, n, rp, ci, vout);
-  PXG_CUDA(c, cudaGetLastError());
-  int32_t tot = 0;
-  PXG_CUDA(c, cudaMemcpyAsync(&tot, rp + n, 4, cudaMemcpyDeviceToHost, s));
+  unsigned const bn = (unsigned)((n + 127) / 128);
+  PXG_CUDA(c, cudaMemsetAsync(c->counter.p, 0, 8, s));
+  kFlagNearZero<<<bn, 128, 0, s>>>(c->rowPtr.p, vals, n, c->counter.p, nullptr, nullptr, 0);
+  unsigned long long nf = 0;
+  PXG_CUDA(c, cudaMemcpyAsync(&nf, c->counter.p, 8, cudaMemcpyDeviceToHost, s));
   PXG_CUDA(c, cudaStreamSynchronize(s));
-  *nnzOut = tot;
+  if (nf == 0)
+    return closeCsr(c, c->rowPtr.p, c->colIdx.p, n, vals, rp, ci, vout, nnzOut, s);
+  if ((st = ensureDofElem(c)) != PXG_OK)
+    return st;
+  DevBuf<double> fixed;
+  DevBuf<int64_t> pos;
+  DevBuf<int32_t> row;
+  PXG_CUDA(c, fixed.alloc(c->nnz));
+  PXG_CUDA(c, pos.alloc(nf));
+  PXG_CUDA(c, row.alloc(nf));
+  PXG_CUDA(c, cudaMemcpyAsync(fixed.p, vals, c->nnz * 8, cudaMemcpyDeviceToDevice, s));
+  PXG_CUDA(c, cudaMemsetAsync(c->counter.p, 0, 8, s));
+  kFlagNearZero<<<bn, 128, 0, s>>>(c->rowPtr.p, vals, n, c->counter.p, pos.p, row.p, (int64_t)nf);
+  RepairArgs ra{};
+  ra.xyz = c->xyz.p;
+  ra.conn = c->conn.p;
+  ra.emap = c->emap.p;
+  ra.rowPtr = c->rowPtr.p;
+  ra.colIdx = c->colIdx.p;
+  ra.kE = c->hasCoef ? c->kE.p : nullptr;
+  ra.bcMask = c->nbc ? c->bcMask.p : nullptr;
+  ra.bcDiag = c->bcDiag;
+  ra.dofElemPtr = c->dofElemPtr.p;
+  ra.dofElem = c->dofElem.p;
+  ra.nops = (int)R->ops.size();
+  for (int o = 0; o < ra.nops; ++o)
+    ra.ops[o] = RefOp{R->ops[o].stiff, R->ops[o].mass, R->ops[o].bc, R->ops[o].sc, R->ops[o].mc};
+  ra.flagged = pos.p;
+  ra.flaggedRow = row.p;
+  ra.nflagged = (int64_t)nf;
+  ra.vals = fixed.p;
+  unsigned const bf = (unsigned)((nf + 127) / 128);
+  switch (c->etype)
+  {
+  case P1TET:
+    kRepairEntries<P1TET><<<bf, 128, 0, s>>>(ra);
+    break;
+  case P2TET:
+    kRepairEntries<P2TET><<<bf, 128, 0, s>>>(ra);
+    break;
+  case Q1HEX:
+    kRepairEntries<Q1HEX><<<bf, 128, 0, s>>>(ra);
+    break;
+  case Q2HEX:
+    kRepairEntries<Q2HEX><<<bf, 128, 0, s>>>(ra);
+    break;
+  }
+  PXG_CUDA(c, cudaGetLastError());
+  return closeCsr(c, c->rowPtr.p, c->colIdx.p, n, fixed.p, rp, ci, vout, nnzOut, s);
+}
+
+pxg_status pxg_get_qpoints(pxg_ctx * c, double * qpts, int mem, void * stream)
+{
+  if (!c || !qpts)
+    return PXG_ERR_INVALID_ARG;
+  if (c->etype < 0)
+    return fail(c, PXG_ERR_INVALID_ARG, "set the mesh first");
+  pxg_status st = ensureDevice(c);
+  if (st != PXG_OK)
+    return st;
+  cudaStream_t const s = (cudaStream_t)stream;
+  size_t const count = (size_t)c->nelem * numQpts(c->etype) * 3;
+  DevBuf<double> tmp;
+  double * out = qpts;
+  if (mem == PXG_MEM_HOST)
+  {
+    PXG_CUDA(c, tmp.alloc(count));
+    out = tmp.p;
+  }
+  unsigned const blocks = (unsigned)((c->nelem + 127) / 128);
+  switch (c->etype)
+  {
+  case P1TET:
+    kQpoints<P1TET><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, out);
+    break;
+  case P2TET:
+    kQpoints<P2TET><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, out);
+    break;
+  case Q1HEX:
+    kQpoints<Q1HEX><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, out);
+    break;
+  case Q2HEX:
+    kQpoints<Q2HEX><<<blocks, 128, 0, s>>>(c->nelem, c->xyz.p, c->conn.p, out);
+    break;
+  }
+  PXG_CUDA(c, cudaGetLastError());
+  if (mem == PXG_MEM_HOST)
+  {
+    PXG_CUDA(c, cudaMemcpyAsync(qpts, out, count * 8, cudaMemcpyDeviceToHost, s));
+    PXG_CUDA(c, cudaStreamSynchronize(s));
+  }
   return PXG_OK;
 }
 

@@ -898,6 +898,7 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
       key.grad[i] = grads[i];
       key.scatter[i] = ctxs[i]->scatter;
       key.threads[i] = ctxs[i]->threads;
+      key.arith[i] = ctxs[i]->arith;
     }
     key.rhs = *rhs;
     key.rtol = rtol;

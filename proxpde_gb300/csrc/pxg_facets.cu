@@ -337,6 +337,8 @@ pxg_status pxg_mark_facets_box(pxg_ctx * c, double const * origin, double const 
 pxg_status pxg_set_bc_markers(pxg_ctx * c, int32_t const * markers, int32_t const * fns, double const * coefs,
                               int nbc, double diag)
 {
+  if (c)
+    ++c->bcVer;
   if (!c || nbc < 0 || (nbc > 0 && (!markers || !fns || !coefs)))
     return PXG_ERR_INVALID_ARG;
   if (c->ndof <= 0)

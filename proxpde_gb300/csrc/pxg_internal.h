@@ -234,13 +234,14 @@ struct GraphKey
   double rtol = 0.;
   int maxIter = 0;
   int scatter[2] = {0, 0}, threads[2] = {0, 0}; // the element kernels captured in the graph
+  int arith[2] = {0, 0};
   bool operator==(GraphKey const & o) const
   {
     return nctx == o.nctx && ctx[0] == o.ctx[0] && ctx[1] == o.ctx[1] && ut[0] == o.ut[0] && ut[1] == o.ut[1] &&
            grad[0] == o.grad[0] && grad[1] == o.grad[1] && rhs.kind == o.rhs.kind && rhs.fn == o.rhs.fn &&
            rhs.coef == o.rhs.coef && rhs.field == o.rhs.field && rtol == o.rtol && maxIter == o.maxIter &&
            scatter[0] == o.scatter[0] && scatter[1] == o.scatter[1] && threads[0] == o.threads[0] &&
-           threads[1] == o.threads[1];
+           threads[1] == o.threads[1] && arith[0] == o.arith[0] && arith[1] == o.arith[1];
   }
 };
 
@@ -317,15 +318,41 @@ struct pxg_ctx
     pxg::DevBuf<uint32_t> face;
     pxg::DevBuf<int32_t> marker;
   } facets;
-  // Q1 hexahedra use the tensor-product kernel in double-float arithmetic; in the
-  // environment PXG_Q1_FP64=1 selects its FP64 variant and PXG_Q1_GENERIC=1 the
-  // generic kernel (both kept for cross-checks)
+  // arithmetic of the element kernels (pxg_set_arithmetic): PXG_ARITH_FP64 (default)
+  // or PXG_ARITH_DFL (double-float, opt-in).  Cross-check kernels, chosen in the
+  // environment when the context is created: PXG_Q1_GENERIC=1 (the per-quadrature-point
+  // FP64 kernel), PXG_Q1_THREAD=1 (the one-thread tensor-product kernel in the
+  // context's arithmetic), PXG_Q1_GROUP=1 (the eight-lanes-per-element kernel in the
+  // context's arithmetic; the double-float default), PXG_TET_GENERIC=1 and
+  // PXG_Q2_GENERIC=1 (the per-quadrature-point FP64 kernels)
+  int arith = PXG_ARITH_FP64;
   bool q1Generic = false;
-  bool q1Fp64 = false;
-  bool tetFp64 = false; // P1/P2: the FP64 element kernel instead of kAssembleTet
-  bool q2Fp64 = false;  // Q2: the FP64 element kernel instead of kAssembleQ2
-  int sms = 0;          // SMs of the device (persistent grids)
   bool q1Thread = false;
+  bool q1Group = false;
+  bool tetGeneric = false;
+  bool q2Generic = false;
+  int sms = 0; // SMs of the device (persistent grids)
+  // What produced each value array pxg_assemble wrote (its recipe): the lhs operators
+  // added into it since it was last overwritten, with the versions of the coordinates,
+  // the coefficient and the BCs they used.  pxg_close_matrix recomputes the array's
+  // near-zero entries in the reference's evaluation order from it (pxg_assemble.cu).
+  struct LhsRec
+  {
+    int stiff, mass, bc;
+    double sc, mc;
+  };
+  struct Recipe
+  {
+    double const * vals = nullptr;
+    std::vector<LhsRec> ops;
+    uint64_t meshVer = 0, coefVer = 0, bcVer = 0;
+    bool valid = false;
+  };
+  std::vector<Recipe> recipes;
+  uint64_t meshVer = 1, coefVer = 1, bcVer = 1;
+  // element ids of each DOF in ascending order (built on the first recomputation)
+  pxg::DevBuf<int32_t> dofElemPtr;
+  pxg::DevBuf<uint32_t> dofElem;
   CgWork cg;
   AdjState adj;
   BatchState batch;
@@ -384,6 +411,8 @@ __device__ __forceinline__ int64_t elemOf(AsmArgs const & a, int64_t i)
 }
 
 void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThread, int threads);
+// the FP64 one-thread-per-element Q1 kernel (pxg_q1f64.cu), the default
+void launchAssembleQ1F64(AsmArgs const & a, cudaStream_t s, int threads);
 // element colouring (pxg_colour.cu); built once per mesh
 pxg_status buildColouring(pxg_ctx * c);
 
@@ -471,9 +500,14 @@ pxg_status initTables(pxg_ctx * c);
 void hostRule(int t, std::vector<double> & xi, std::vector<double> & w);
 pxg_status initQ2Tables(pxg_ctx * c);                      // pxg_q2.cu
 void launchAssembleQ2(AsmArgs const & a, cudaStream_t s, int sms); // pxg_q2.cu
+pxg_status initQ2F64Tables(pxg_ctx * c);                          // pxg_q2f64.cu
+void launchAssembleQ2F64(AsmArgs const & a, cudaStream_t s);      // pxg_q2f64.cu
 void hostShape(int t, double const * p, double * phi, double * dphi);
 // g_e = -(C u)_e^T K_e (C lambda)_e for every element (pxg_assemble.cu)
 pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, double * g, cudaStream_t s);
+// prune + compaction of a structural CSR into caller buffers (pxg_assemble.cu)
+pxg_status closeCsr(pxg_ctx * c, int32_t const * rowPtr, int32_t const * colIdx, int64_t n, double const * vals,
+                    int32_t * rp, int32_t * ci, double * vout, int64_t * nnzOut, cudaStream_t s);
 // Jacobi-PCG (pxg_solve.cu)
 pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double const * a, int64_t n,
                    double const * b, double * x, double rtol, int maxIter, int * itersOut, double * relOut,

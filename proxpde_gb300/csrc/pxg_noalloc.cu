@@ -14,8 +14,9 @@
 //   - the scratch array (16.8 MB) is held on every GPU that loads the library until
 //     the process exits;
 //   - the first call on a device looks up the array's device address (set-up once per
-//     device, with that device current); make that first call before any stream
-//     capture;
+//     device, with that device current);
+//   - every call copies the kept count back to the host and synchronises `stream`
+//     before it returns, so a call cannot be captured into a CUDA graph;
 //   - every call shares the one array: calls that overlap on the GPU (different
 //     streams or threads) race and corrupt each other's result; serialise them;
 //   - the array keeps the last call's contents; each call writes every entry it later

@@ -1234,10 +1234,9 @@ void launchAssembleQ1(AsmArgs const & a, cudaStream_t s, bool fp64, bool perThre
     unsigned const blocks = (unsigned)((a.nelem * 8 + nt - 1) / nt);
     kern<<<blocks, nt, smem, s>>>(a);
   };
-  int const nt = threads ? threads : q1g::kThreads;
   if (fp64)
-    go(q1g::kAssembleQ1Group<double, q1g::kThreads>, q1g::kThreads, q1g::smemBytes<q1g::kThreads>());
-  else if (nt == 512)
+    go(q1g::kAssembleQ1Group<double, 256>, 256, q1g::smemBytes<256>());
+  else if (threads == 512)
     go(q1g::kAssembleQ1Group<dfl, 512>, 512, q1g::smemBytes<512>());
   else
     go(q1g::kAssembleQ1Group<dfl, 256>, 256, q1g::smemBytes<256>());

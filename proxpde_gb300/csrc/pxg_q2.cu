@@ -386,7 +386,7 @@ pxg_status initQ2Tables(pxg_ctx * c)
   PXG_CUDA(c, cudaMemcpyToSymbol(gXi, xi.data(), xi.size() * sizeof(double)));
   PXG_CUDA(c, cudaMemcpyToSymbol(gW, w.data(), w.size() * sizeof(double)));
   PXG_CUDA(c, cudaMemcpyToSymbol(gPairs, pairs.data(), pairs.size() * sizeof(uint16_t)));
-  return PXG_OK;
+  return initQ2F64Tables(c);
 }
 
 void launchAssembleQ2(AsmArgs const & a, cudaStream_t s, int sms)

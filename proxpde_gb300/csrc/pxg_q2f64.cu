@@ -1,0 +1,470 @@
+// Q2 hexahedron element kernel in FP64 arithmetic with sum factorisation: one warp per
+// element.  It computes what proxpde's element loop computes for a Q2 hexahedron with
+// the 3x3x3 Gauss rule (include/builder.hpp:53-153): CurFE::reinit (include/curfe.hpp:
+// 50-103), AssemblyStiffness(FE) / AssemblyScalarMass / AssemblyMassFE
+// (include/assembly_lhs.hpp:52-109, 207-221, 262-277), AssemblyRhsAnalytic and
+// AssemblyS2SProjection (include/assembly_rhs.hpp:61-88, 130-159) and the Dirichlet
+// condensation (builder.hpp:76-124), in IEEE binary64, with FP64 reductions into the
+// CSR values and the load vector.
+//
+// The Q2 basis is a tensor product of the 1D functions l_0 = x(x-1)/2, l_1 = x(x+1)/2,
+// l_2 = 1 - x^2 (src/reffe.cpp:374-383), and the rule a tensor product of the 3-point
+// Gauss rule, so every sum over the 27 points factors into three 3-term sums:
+//  - per point (lane q): J of the trilinear map from the Walsh-Hadamard transform of
+//    the vertices (the 27 mapping points lie on the trilinear image, so this is the
+//    reference's J), J^T J, its adjugate and determinant D, 1/|det J| = rsqrt(D) (one
+//    third-order Newton step), w_q |det J_q|, G_q = k w_q |det J| (J^T J)^-1;
+//  - stiffness tables, each three one-axis contractions of one G component with the
+//    1D products D_ab = l'_a l'_b, P_ab = l_a l_b (6 symmetric classes) or
+//    E_ab = l'_a l_b (9): S_x = sum G_xx D P P, S_y, S_z (216 values each) and
+//    U_xy = sum G_xy E E P, U_xz, U_yz (486 each); an entry K_ij is a sum of nine
+//    table values (three S, two of each U);
+//  - mass table sum |det J| w P P P (216), M_ij one value of it;
+//  - the load r_q = w_q |det J_q| f(qpoint_q), contracted to the nodes with l_a.
+// About 16k FP64 operations per element against about 100k for the per-point form.
+// A contraction stage maps [3][m] (point axis first) to [m][C] (C classes last), so
+// three stages turn [qx][qy][qz] into [cx][cy][cz]; the lanes take the stage's outputs
+// in turn.
+#include <vector>
+
+#include "pxg_internal.h"
+
+namespace pxg
+{
+namespace q2f
+{
+constexpr int NQ = 27, N = 27, NP = N * (N + 1) / 2;
+
+// 1D tables at the three Gauss points t_0 < t_1 = 0 < t_2 (from initQ2F64Tables):
+// [0, 9) l_a(t_k) at 3a + k; [9, 27) P classes; [27, 45) D classes; [45, 72) E_ab at
+// 3(3a + b) + k.  Symmetric classes: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2).
+__device__ double gCoef[72];
+__device__ double gT[3];           // t_k
+__device__ double gWl[NQ];         // weights in lattice order qx * 9 + qy * 3 + qz
+__device__ uint8_t gRuleOfLat[NQ]; // the rule's point index of each lattice point
+__device__ uint8_t gLatOfNode[N];  // node n -> ax * 9 + ay * 3 + az (1D function indices)
+__device__ uint8_t gNodeOfLat[N];
+__device__ uint16_t gPairsF[NP];   // (i << 8 | j), i <= j
+
+constexpr int kTab = 3 * 216 + 3 * 486; // S_x S_y S_z U_xy U_xz U_yz
+
+__host__ __device__ constexpr int symCls(int a, int b)
+{
+  return a == b ? a : (a + b == 1 ? 3 : (a + b == 2 ? 4 : 5));
+}
+
+// 1/sqrt(x) by the hardware estimate and one third-order Newton step
+__device__ __forceinline__ double rsqrtN(double x)
+{
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double const e = fma(-(x * y), y, 1.0);
+  return fma(y * e, fma(0.375, e, 0.5), y);
+}
+
+// out[r * C + c] = sum_k coef[3c + k] in[k * m + r] (r < m, c < C), lanes in turn
+__device__ __forceinline__ void stage(double const * in, int m, int C, double const * coef, double * out, int lane)
+{
+  for (int o = lane; o < m * C; o += 32)
+  {
+    int const r = o / C, c = o - r * C;
+    double const * k = coef + 3 * c;
+    out[o] = fma(k[2], in[2 * m + r], fma(k[1], in[m + r], k[0] * in[r]));
+  }
+  __syncwarp();
+}
+// three stages of a [3][3][3] array with the coefficient tables of the three axes
+__device__ __forceinline__ void contract3(double const * in, int c0, double const * k0, int c1, double const * k1,
+                                          int c2, double const * k2, double * out, double * scr0, double * scr1,
+                                          int lane)
+{
+  stage(in, 9, c0, k0, scr0, lane);       // [3][3][c0]
+  stage(scr0, 3 * c0, c1, k1, scr1, lane); // [3][c0][c1]
+  stage(scr1, c0 * c1, c2, k2, out, lane); // [c0][c1][c2]
+}
+
+__device__ __noinline__ void condenseF(double * pij, double bcDiag, double * b, uint32_t dofi, uint32_t dofj,
+                                       double bvi, double bvj, bool ci, bool cj, bool isDiag, double val)
+{
+  if (isDiag)
+  {
+    atomicAdd(pij, bcDiag);
+    return;
+  }
+  if (!b)
+    return;
+  if (!ci)
+  {
+    double const t = val * bvj;
+    if (t != 0.)
+      atomicAdd(b + dofi, -t);
+  }
+  if (!cj)
+  {
+    double const t = val * bvi;
+    if (t != 0.)
+      atomicAdd(b + dofj, -t);
+  }
+}
+
+// f at the point, out of line (its FP64 code is only run for the load)
+__device__ __noinline__ double evalPoint(int fn, double rc, double x, double y, double z)
+{
+  return evalFn(fn, rc, x, y, z);
+}
+
+struct Smem
+{
+  double coef[72];
+  double w[NQ];
+  double X[8][3];
+  double G[6][NQ];
+  double ad[NQ];
+  double Mt[216];
+  double tab[kTab];
+  double scr[2][243];
+  double bv[N];
+  uint32_t dof[N];
+  int32_t rp[N];
+  uint8_t latOfNode[N];
+  uint8_t nodeOfLat[N];
+  uint8_t ruleOfLat[NQ];
+};
+} // namespace q2f
+
+__global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
+{
+  using namespace q2f;
+  __shared__ Smem S;
+  int const lane = threadIdx.x;
+  for (int k = lane; k < 72; k += 32)
+    S.coef[k] = gCoef[k];
+  if (lane < NQ)
+  {
+    S.w[lane] = gWl[lane];
+    S.latOfNode[lane] = gLatOfNode[lane];
+    S.nodeOfLat[lane] = gNodeOfLat[lane];
+    S.ruleOfLat[lane] = gRuleOfLat[lane];
+  }
+  int64_t const e = elemOf(a, blockIdx.x);
+  // ---- inputs
+  if (lane < 24)
+  {
+    uint32_t const id = a.conn[e * 8 + lane / 3];
+    S.X[lane / 3][lane % 3] = a.xyz[3 * (int64_t)id + lane % 3];
+  }
+  bool mine = false;
+  if (lane < N)
+  {
+    uint32_t const d = a.emap[e * N + lane];
+    S.dof[lane] = d;
+    S.rp[lane] = a.rowPtr[d];
+    mine = a.bcMask && a.bcMask[d];
+    S.bv[lane] = mine ? a.bcVal[d] : 0.;
+  }
+  uint32_t const cons = __ballot_sync(0xffffffffu, mine);
+  __syncwarp();
+  LhsDev const & op0 = a.op[0];
+  LhsDev const & op1 = a.op[1];
+  bool const k0 = op0.on && op0.stiff, k1 = op1.on && op1.stiff;
+  bool const m0 = op0.on && op0.mass, m1 = op1.on && op1.mass;
+  bool const needK = k0 || k1, needM = m0 || m1;
+  double const kfac = ((usesCoef(op0) || usesCoef(op1)) && a.kE) ? a.kE[e] : 1.0;
+  bool const foldK = k0 != k1, foldM = m0 != m1;
+  double const ks0 = k0 ? (op0.stiff == 2 ? op0.sc * kfac : op0.sc) : 0.;
+  double const ks1 = k1 ? (op1.stiff == 2 ? op1.sc * kfac : op1.sc) : 0.;
+  double const ms0 = m0 ? massCoef(op0, kfac) : 0., ms1 = m1 ? massCoef(op1, kfac) : 0.;
+
+  // ---- per point: lane q = qx * 9 + qy * 3 + qz.  Walsh-Hadamard transform of the
+  // vertices (every lane, same values): x(xi) = 1/8 sum_k H_k xi^kx eta^ky zeta^kz;
+  // the Jacobian columns (x8) c1 = H100 + eta H110 + zeta H101 + eta zeta H111, ...
+  if (lane < NQ)
+  {
+    int const qx = lane / 9, qy = (lane / 3) % 3, qz = lane % 3;
+    double const xi = gT[qx], eta = gT[qy], zeta = gT[qz];
+    double c[3][3]; // c[col][r]
+    double o[3];    // the element origin, the vertex average (geo.hpp:721-728)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+    {
+      // vertex v at lattice (vx, vy, vz): proxpde's Q1 vertex order (src/reffe.cpp:684-759)
+      double H[2][2][2];
+#pragma unroll
+      for (int v = 0; v < 8; ++v)
+      {
+        int const vx = (v == 1 || v == 2 || v == 5 || v == 6), vy = (v == 2 || v == 3 || v == 6 || v == 7), vz = v >= 4;
+        H[vx][vy][vz] = S.X[v][r];
+      }
+#pragma unroll
+      for (int y = 0; y < 2; ++y)
+#pragma unroll
+        for (int z = 0; z < 2; ++z)
+        {
+          double const p0 = H[0][y][z], p1 = H[1][y][z];
+          H[0][y][z] = p0 + p1, H[1][y][z] = p1 - p0;
+        }
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int z = 0; z < 2; ++z)
+        {
+          double const p0 = H[x][0][z], p1 = H[x][1][z];
+          H[x][0][z] = p0 + p1, H[x][1][z] = p1 - p0;
+        }
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+        {
+          double const p0 = H[x][y][0], p1 = H[x][y][1];
+          H[x][y][0] = p0 + p1, H[x][y][1] = p1 - p0;
+        }
+      c[0][r] = fma(zeta, fma(eta, H[1][1][1], H[1][0][1]), fma(eta, H[1][1][0], H[1][0][0]));
+      c[1][r] = fma(zeta, fma(xi, H[1][1][1], H[0][1][1]), fma(xi, H[1][1][0], H[0][1][0]));
+      c[2][r] = fma(eta, fma(xi, H[1][1][1], H[0][1][1]), fma(xi, H[1][0][1], H[0][0][1]));
+      o[r] = 0.125 * H[0][0][0];
+    }
+    double const g11 = fma(c[0][0], c[0][0], fma(c[0][1], c[0][1], c[0][2] * c[0][2]));
+    double const g22 = fma(c[1][0], c[1][0], fma(c[1][1], c[1][1], c[1][2] * c[1][2]));
+    double const g33 = fma(c[2][0], c[2][0], fma(c[2][1], c[2][1], c[2][2] * c[2][2]));
+    double const g12 = fma(c[0][0], c[1][0], fma(c[0][1], c[1][1], c[0][2] * c[1][2]));
+    double const g13 = fma(c[0][0], c[2][0], fma(c[0][1], c[2][1], c[0][2] * c[2][2]));
+    double const g23 = fma(c[1][0], c[2][0], fma(c[1][1], c[2][1], c[1][2] * c[2][2]));
+    double const A11 = fma(-g23, g23, g22 * g33);
+    double const A22 = fma(-g13, g13, g11 * g33);
+    double const A33 = fma(-g12, g12, g11 * g22);
+    double const A12 = fma(g13, g23, -(g12 * g33));
+    double const A13 = fma(g12, g23, -(g13 * g22));
+    double const A23 = fma(g12, g13, -(g11 * g23));
+    double const D = fma(g11, A11, fma(g12, A12, g13 * A13));
+    double const rs = rsqrtN(D);
+    double const wq = S.w[lane];
+    S.ad[lane] = (D * rs) * wq; // w |det J| x 512
+    // k w |det J| (J^T J)^-1 = k w adj rsqrt(D) / 8 (the columns carry x8)
+    double const sG = ((foldK ? (k0 ? ks0 : ks1) : 1.0) * 0.125) * (wq * rs);
+    S.G[0][lane] = sG * A11, S.G[1][lane] = sG * A22, S.G[2][lane] = sG * A33;
+    S.G[3][lane] = sG * A12, S.G[4][lane] = sG * A13, S.G[5][lane] = sG * A23;
+    // the qpoint origin + J xi (curfe.hpp:80), for the analytic load
+    if (a.rkind == 1)
+    {
+      double const x = fma(0.125, fma(xi, c[0][0], fma(eta, c[1][0], zeta * c[2][0])), o[0]);
+      double const y = fma(0.125, fma(xi, c[0][1], fma(eta, c[1][1], zeta * c[2][1])), o[1]);
+      double const z = fma(0.125, fma(xi, c[0][2], fma(eta, c[1][2], zeta * c[2][2])), o[2]);
+      S.scr[0][lane] = x, S.scr[0][32 + lane] = y, S.scr[0][64 + lane] = z;
+    }
+  }
+  __syncwarp();
+  double const * const cL = S.coef;
+  double const * const cP = S.coef + 9;
+  double const * const cD = S.coef + 27;
+  double const * const cE = S.coef + 45;
+
+  // ---- load vector (buildLhs' BC values, buildRhs)
+  bool const bcOps = (op0.on && op0.bc) || (op1.on && op1.bc);
+  if (a.b && cons && bcOps && lane < N && ((cons >> lane) & 1u))
+  {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+      if (a.op[m].on && a.op[m].bc && S.bv[lane] != 0.)
+        atomicAdd(a.b + S.dof[lane], S.bv[lane]);
+  }
+  if (a.rkind)
+  {
+    // r_q = w_q |det J_q| f_q (x512: the 1/512 is in rc), then Fe = sum_q r_q l l l
+    double const rc = a.rc * (1. / 512.);
+    double * const rq = S.scr[1];
+    if (lane < NQ)
+    {
+      double f;
+      if (a.rkind == 1)
+        f = evalPoint(a.fn, rc, S.scr[0][lane], S.scr[0][32 + lane], S.scr[0][64 + lane]);
+      else if (a.rkind == 3)
+        f = rc * a.field[e * NQ + S.ruleOfLat[lane]];
+      else
+      {
+        // projection: the field at the point, sum_n phi_n(q) field_n with phi_n = l l l
+        int const qx = lane / 9, qy = (lane / 3) % 3, qz = lane % 3;
+        double s = 0.;
+        for (int n = 0; n < N; ++n)
+        {
+          int const L = S.latOfNode[n];
+          s = fma(cL[3 * (L / 9) + qx] * cL[3 * ((L / 3) % 3) + qy] * cL[3 * (L % 3) + qz], a.field[S.dof[n]], s);
+        }
+        f = rc * s;
+      }
+      rq[lane] = S.ad[lane] * f;
+    }
+    __syncwarp();
+    double * const bn = S.scr[0] + 96; // [ax][ay][az]
+    stage(rq, 9, 3, cL, S.scr[0], lane);
+    stage(S.scr[0], 9, 3, cL, S.scr[0] + 128, lane);
+    stage(S.scr[0] + 128, 9, 3, cL, bn, lane);
+    if (lane < N)
+    {
+      int const n = S.nodeOfLat[lane];
+      if (!(a.rbc && ((cons >> n) & 1u)))
+        atomicAdd(a.b + S.dof[n], bn[lane]);
+    }
+    __syncwarp();
+  }
+
+  // ---- mass table: w |det J| (times a single mass operator's coefficient, and the
+  // 1/512) contracted with P over the three axes
+  if (needM)
+  {
+    double const mcf = (foldM ? (m0 ? ms0 : ms1) : 1.0) * (1. / 512.);
+    if (lane < NQ)
+      S.scr[1][lane] = mcf * S.ad[lane];
+    __syncwarp();
+    contract3(S.scr[1], 6, cP, 6, cP, 6, cP, S.Mt, S.scr[0], S.tab, lane);
+  }
+  // ---- stiffness tables
+  double * const tSx = S.tab;
+  double * const tSy = S.tab + 216;
+  double * const tSz = S.tab + 432;
+  double * const tUxy = S.tab + 648;
+  double * const tUxz = S.tab + 648 + 486;
+  double * const tUyz = S.tab + 648 + 972;
+  if (needK)
+  {
+    contract3(S.G[0], 6, cD, 6, cP, 6, cP, tSx, S.scr[0], S.scr[1], lane);
+    contract3(S.G[1], 6, cP, 6, cD, 6, cP, tSy, S.scr[0], S.scr[1], lane);
+    contract3(S.G[2], 6, cP, 6, cP, 6, cD, tSz, S.scr[0], S.scr[1], lane);
+    contract3(S.G[3], 9, cE, 9, cE, 6, cP, tUxy, S.scr[0], S.scr[1], lane); // [ex][ey][pz]
+    contract3(S.G[4], 9, cE, 6, cP, 9, cE, tUxz, S.scr[0], S.scr[1], lane); // [ex][py][ez]
+    contract3(S.G[5], 6, cP, 9, cE, 9, cE, tUyz, S.scr[0], S.scr[1], lane); // [px][ey][ez]
+  }
+
+  // ---- entries i <= j and the scatter
+  uint16_t const * rk = a.rank + e * (int64_t)(N * N);
+  bool const anyBc = cons && bcOps;
+  for (int p = lane; p < NP; p += 32)
+  {
+    uint16_t const pr = gPairsF[p];
+    int const i = pr >> 8, j = pr & 0xff;
+    int const Li = S.latOfNode[i], Lj = S.latOfNode[j];
+    int const ix = Li / 9, iy = (Li / 3) % 3, iz = Li % 3, jx = Lj / 9, jy = (Lj / 3) % 3, jz = Lj % 3;
+    int const px = symCls(ix, jx), py = symCls(iy, jy), pz = symCls(iz, jz);
+    double kv = 0., mv = 0.;
+    if (needK)
+    {
+      kv = tSx[px * 36 + py * 6 + pz] + tSy[px * 36 + py * 6 + pz];
+      kv += tSz[px * 36 + py * 6 + pz];
+      // the S tables share the index because D and P use the same symmetric classes
+      kv += tUxy[(3 * ix + jx) * 54 + (3 * jy + iy) * 6 + pz] + tUxy[(3 * jx + ix) * 54 + (3 * iy + jy) * 6 + pz];
+      kv += tUxz[(3 * ix + jx) * 54 + py * 9 + (3 * jz + iz)] + tUxz[(3 * jx + ix) * 54 + py * 9 + (3 * iz + jz)];
+      kv += tUyz[px * 81 + (3 * iy + jy) * 9 + (3 * jz + iz)] + tUyz[px * 81 + (3 * jy + iy) * 9 + (3 * iz + jz)];
+    }
+    if (needM)
+      mv = S.Mt[px * 36 + py * 6 + pz];
+    int32_t const pij = S.rp[i] + rk[i * N + j], pji = S.rp[j] + rk[j * N + i];
+    bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+    {
+      LhsDev const & op = a.op[m];
+      if (!op.on)
+        continue;
+      double val;
+      if (op.stiff)
+      {
+        val = foldK ? kv : (m ? ks1 : ks0) * kv;
+        if (op.mass)
+          val = foldM ? val + mv : fma(m ? ms1 : ms0, mv, val);
+      }
+      else
+        val = foldM ? mv : (m ? ms1 : ms0) * mv;
+      if (anyBc && op.bc && (ci || cj))
+      {
+        condenseF(op.vals + pij, a.bcDiag, a.b, S.dof[i], S.dof[j], S.bv[i], S.bv[j], ci, cj, i == j, val);
+        continue;
+      }
+      atomicAdd(op.vals + pij, val);
+      if (i != j)
+        atomicAdd(op.vals + pji, val);
+    }
+  }
+}
+
+// The 1D tables, the lattice maps and the pair list, from the reference's rule and
+// basis (the engine's host restatement of src/qr.cpp and src/reffe.cpp).
+pxg_status initQ2F64Tables(pxg_ctx * c)
+{
+  using namespace q2f;
+  std::vector<double> xi, w;
+  hostRule(Q2HEX, xi, w);
+  if ((int)w.size() != NQ)
+    return fail(c, PXG_ERR_UNSUPPORTED, "Q2 rule: %d points", (int)w.size());
+  // the three 1D points, ascending
+  double t[3] = {1e300, 0., -1e300};
+  for (int q = 0; q < NQ; ++q)
+  {
+    t[0] = xi[3 * q] < t[0] ? xi[3 * q] : t[0];
+    t[2] = xi[3 * q] > t[2] ? xi[3 * q] : t[2];
+  }
+  auto idx = [&](double v) { return v == t[0] ? 0 : (v == t[2] ? 2 : 1); };
+  t[1] = 0.;
+  double wl[NQ];
+  uint8_t ruleOfLat[NQ];
+  for (int q = 0; q < NQ; ++q)
+  {
+    int const L = idx(xi[3 * q]) * 9 + idx(xi[3 * q + 1]) * 3 + idx(xi[3 * q + 2]);
+    wl[L] = w[q];
+    ruleOfLat[L] = (uint8_t)q;
+  }
+  // 1D functions of src/reffe.cpp:374-383 (index 0: node -1, 1: node +1, 2: node 0)
+  auto f = [](int a, double x) { return a == 0 ? 0.5 * x * (x - 1.) : (a == 1 ? 0.5 * x * (x + 1.) : 1. - x * x); };
+  auto df = [](int a, double x) { return a == 0 ? x - 0.5 : (a == 1 ? x + 0.5 : -2. * x); };
+  int const cls[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  std::vector<double> coef(72);
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < 3; ++k)
+      coef[3 * a + k] = f(a, t[k]);
+  for (int cc = 0; cc < 6; ++cc)
+    for (int k = 0; k < 3; ++k)
+    {
+      coef[9 + 3 * cc + k] = f(cls[cc][0], t[k]) * f(cls[cc][1], t[k]);
+      coef[27 + 3 * cc + k] = df(cls[cc][0], t[k]) * df(cls[cc][1], t[k]);
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      for (int k = 0; k < 3; ++k)
+        coef[45 + 3 * (3 * a + b) + k] = df(a, t[k]) * f(b, t[k]);
+  // node n -> the 1D functions of its three factors: the lattice point where phi_n = 1
+  uint8_t latOfNode[N], nodeOfLat[N];
+  double const node1d[3] = {-1., 1., 0.};
+  for (int L = 0; L < N; ++L)
+  {
+    double const p[3] = {node1d[L / 9], node1d[(L / 3) % 3], node1d[L % 3]};
+    double phi[N], dphi[3 * N];
+    hostShape(Q2HEX, p, phi, dphi);
+    int found = -1;
+    for (int n = 0; n < N; ++n)
+      if (phi[n] > 0.5)
+        found = n;
+    if (found < 0)
+      return fail(c, PXG_ERR_UNSUPPORTED, "Q2 node lattice");
+    latOfNode[found] = (uint8_t)L;
+    nodeOfLat[L] = (uint8_t)found;
+  }
+  std::vector<uint16_t> pairs;
+  for (int i = 0; i < N; ++i)
+    for (int j = i; j < N; ++j)
+      pairs.push_back((uint16_t)(i << 8 | j));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gCoef, coef.data(), 72 * 8));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gT, t, 24));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gWl, wl, NQ * 8));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gRuleOfLat, ruleOfLat, NQ));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gLatOfNode, latOfNode, N));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gNodeOfLat, nodeOfLat, N));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gPairsF, pairs.data(), pairs.size() * 2));
+  return PXG_OK;
+}
+
+void launchAssembleQ2F64(AsmArgs const & a, cudaStream_t s)
+{
+  if (a.nelem > 0)
+    kAssembleQ2F64<<<(unsigned)a.nelem, 32, 0, s>>>(a);
+}
+
+} // namespace pxg

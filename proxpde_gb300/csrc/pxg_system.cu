@@ -486,6 +486,15 @@ pxg_status pxg_sys_get_pattern(pxg_sys * s, int32_t * row_ptr, int32_t * col_idx
   return PXG_OK;
 }
 
+pxg_status pxg_sys_close_matrix(pxg_sys * s, double const * vals, int32_t * row_ptr, int32_t * col_idx,
+                                double * vals_out, int64_t * nnz_out, void * stream)
+{
+  if (!s || !vals || !row_ptr || !col_idx || !vals_out || !nnz_out)
+    return PXG_ERR_INVALID_ARG;
+  return closeCsr(s->sp[0], s->rowPtr.p, s->colIdx.p, s->ntot, vals, row_ptr, col_idx, vals_out, nnz_out,
+                  (cudaStream_t)stream);
+}
+
 pxg_status pxg_sys_pattern_device(pxg_sys * s, int32_t const ** row_ptr, int32_t const ** col_idx)
 {
   if (!s || !row_ptr || !col_idx)

@@ -39,3 +39,18 @@ def engine():
 
     px.load()
     return px
+
+
+def pytest_terminal_summary(terminalreporter):
+    """The largest entrywise relative error of each named engine-vs-oracle comparison,
+    over the entries above 1e-3 and above 1e-8 of their row's largest, one line each."""
+    try:
+        from helpers import ERRORS
+    except ImportError:
+        return
+    if not ERRORS:
+        return
+    terminalreporter.write_sep("-", "entrywise relative error against the oracle (entries >= 1e-3 / >= 1e-8 "
+                                    "of their row's largest)")
+    for k in sorted(ERRORS):
+        terminalreporter.write_line(f"{k}: {ERRORS[k][0]:.3e} / {ERRORS[k][1]:.3e}")

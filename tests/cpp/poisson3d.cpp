@@ -14,8 +14,11 @@ template <int Order>
 int run(int n, char const * out)
 {
   using namespace proxgpu;
+  using Mesh_T = Mesh<Hexahedron>;
+  using FESpace_T =
+      FESpace<Mesh_T, typename LagrangeFE<Hexahedron, Order>::RefFE_T, typename LagrangeFE<Hexahedron, Order>::RecommendedQR>;
   auto const mesh = buildHyperCube<Hexahedron>(n);
-  FESpace<Hexahedron, Order> feSpace{mesh};
+  FESpace_T feSpace{mesh};
   auto const bcs = std::vector{BCEss{feSpace, side::LEFT}, BCEss{feSpace, side::BOTTOM}};
   Builder builder{feSpace};
   builder.buildLhs(std::tuple{AssemblyStiffness(1.0, feSpace)}, bcs);

@@ -14,9 +14,12 @@ template <typename Elem_T>
 int run(char const * out)
 {
   double const ly = 2.;
-  auto const mesh = buildHyperCube<Elem_T>({0., 0., 0.}, {1., ly, 1.}, 4);
-  FESpace<Elem_T, 2, 3> feSpaceVel{mesh};
-  FESpace<Elem_T, 1, 1, 2> feSpaceP{mesh, 3 * feSpaceVel.dof.size};
+  using Mesh_T = Mesh<Elem_T>;
+  using QR = typename LagrangeFE<Elem_T, 2>::RecommendedQR;
+  Mesh_T mesh;
+  buildHyperCube(mesh, {0., 0., 0.}, {1., ly, 1.}, {4, 4, 4});
+  FESpace<Mesh_T, typename LagrangeFE<Elem_T, 2>::RefFE_T, QR, 3> feSpaceVel{mesh};
+  FESpace<Mesh_T, typename LagrangeFE<Elem_T, 1>::RefFE_T, QR> feSpaceP{mesh, 3 * feSpaceVel.dof.size};
 
   auto const zero = [](Vec3 const &) { return Vec3::Constant(0.); };
   auto const inlet = [](Vec3 const & p) { return Vec3(0., 0.5 * (1. - p(0) * p(0)), 0.); };

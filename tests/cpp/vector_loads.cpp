@@ -19,9 +19,11 @@ using namespace proxgpu;
 template <typename Elem_T>
 int run(char const * out)
 {
+  using Mesh_T = Mesh<Elem_T>;
   auto const mesh = buildHyperCube<Elem_T>(3);
-  FESpace<Elem_T, 2, 3> feSpaceVel{mesh};
-  FESpace<Elem_T, 1> feSpaceP{mesh, 3 * feSpaceVel.dof.size};
+  FESpace<Mesh_T, typename LagrangeFE<Elem_T, 2>::RefFE_T, typename LagrangeFE<Elem_T, 2>::RecommendedQR, 3> feSpaceVel{mesh};
+  FESpace<Mesh_T, typename LagrangeFE<Elem_T, 1>::RefFE_T, typename LagrangeFE<Elem_T, 1>::RecommendedQR> feSpaceP{
+      mesh, 3 * feSpaceVel.dof.size};
   auto const dofU = feSpaceVel.dof.size;
   auto const dofP = feSpaceP.dof.size;
 

@@ -1,8 +1,9 @@
 """Generates the committed golden fixtures under tests/golden/.
 
-Run in a container where the proxpde sources are mounted (default path below):
+Run where a proxpde checkout is available, giving its path as the argument or in
+the environment variable PROXPDE_SRC:
 
-    python tests/golden/make_golden.py [/path/to/proxpde]
+    python tests/golden/make_golden.py /path/to/proxpde
 
 Fixtures written:
   cube_uns.npz  - the unstructured tetrahedral unit cube of proxpde's
@@ -56,7 +57,10 @@ def read_gmsh22(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    """python make_golden.py <proxpde checkout>, or with PROXPDE_SRC set to it."""
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PROXPDE_SRC")
+    if not ref:
+        sys.exit("usage: make_golden.py <proxpde checkout> (or set PROXPDE_SRC)")
     out = os.path.dirname(os.path.abspath(__file__))
     xyz, tets, tris, tags = read_gmsh22(os.path.join(ref, "data", "cube_uns.msh"))
     np.savez_compressed(os.path.join(out, "cube_uns.npz"), xyz=xyz, tets=tets, tris=tris, tri_tags=tags)

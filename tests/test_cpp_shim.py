@@ -13,9 +13,10 @@ SRC = os.path.join(ROOT, "tests", "cpp", "poisson3d.cpp")
 
 STOKES = os.path.join(ROOT, "tests", "cpp", "stokes3d.cpp")
 LOADS = os.path.join(ROOT, "tests", "cpp", "vector_loads.cpp")
+PORT = os.path.join(ROOT, "tests", "cpp", "poisson3dhex_port.cpp")
 
 
-@pytest.mark.parametrize("src", [SRC, STOKES, LOADS], ids=["poisson3d", "stokes3d", "vector_loads"])
+@pytest.mark.parametrize("src", [SRC, STOKES, LOADS, PORT], ids=["poisson3d", "stokes3d", "vector_loads", "port"])
 def test_shim_compiles(tmp_path, src):
     r = subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
                         src], capture_output=True, text=True)
@@ -118,3 +119,22 @@ def test_shim_vector_loads(engine, tmp_path, elem):
     mesh = buildHyperCube(Hexahedron if elem == "hex" else Tetrahedron, 3)
     expect, _ = vector_load_expect(elem, mesh.xyz, mesh.conn, vector_load_field(3 * ndu))
     assert_close(b, expect, what="shim vector and scalar loads")
+
+
+@pytest.mark.gpu
+def test_shim_port_of_poisson3dhex(engine, tmp_path):
+    """proxpde's test/poisson3dhex.cpp body on the shim with the namespace changed
+    (buildHyperCube(mesh, origin, length, {n,n,n}), FESpace<Mesh_T, RefFE_T, QR_T>,
+    BCEss << lambda, Builder{dof.size}, the rhs as a host lambda, LUSolver on the device
+    CG, interpolateAnalyticFunction of a lambda, checkError): exit code 0 means the
+    golden norm 0.1352139631934435 (test/poisson3dhex.cpp:118) is met to 1e-12."""
+    from proxpde_gb300 import build
+
+    lib = build.build()
+    exe = tmp_path / "poisson3dhex_port"
+    r = subprocess.run(["g++", "-std=c++20", "-O2", "-I", os.path.join(ROOT, "include"), PORT, "-o", str(exe),
+                        f"-L{os.path.dirname(lib)}", "-lpxg", f"-Wl,-rpath,{os.path.dirname(lib)}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), "4", "0.1352139631934435"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -1,7 +1,11 @@
-"""Checks at the full sizes of the reference workloads, through properties that need no
-entry-by-entry comparison (the oracle covers that at smaller sizes):
+"""Checks at the full sizes of the reference workloads:
 
-- the Q1 128^3 stiffness + mass + sin load (the benchmark workload) and the P2 64^3
+- entry by entry against the oracle (threaded over the host's cores): the Q1 128^3
+  K(k_e), M and sin3 load, and the P2 64^3 x 6 K(k_e) and M, each in the default FP64
+  arithmetic and in the opt-in double-float one, with the normwise and entrywise
+  tolerances of tests/helpers.py (1e-12 relative to each entry above the round-off
+  floor of its row);
+- through properties that hold at any size: the Q1 128^3 stiffness + mass + sin load (the benchmark workload) and the P2 64^3
   (6 Kuhn tetrahedra per cell) stiffness + mass: DOF and nnz counts against closed
   forms, a sorted, structurally symmetric pattern with every diagonal, K 1 = 0
   (partition of unity), x^T K x = sum_e k_e vol_e for each coordinate function x and
@@ -21,7 +25,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import nnz_p2_kuhn6, nnz_q1_cube, q1_quadrature
+from helpers import assert_close, compare_csr, gpu_assemble, nnz_p2_kuhn6, nnz_q1_cube, oracle_lhs, q1_quadrature
 
 pytestmark = pytest.mark.gpu
 
@@ -147,6 +151,59 @@ def test_p2_64_cube(engine):
     operator_checks(O.P2TET, xyz, conn, k, ndof, rp, ci, K, M, em, kvol)
     bs = float(b.sum())
     assert abs(bs - 1.0) <= 1e-12, bs  # sum of the load vector of f = 1 is the volume
+
+
+def _threads():
+    import os
+
+    return max(1, len(os.sched_getaffinity(0)))
+
+
+@pytest.mark.parametrize("arith", ["fp64", "dfl"])
+def test_q1_128_entrywise(engine, arith):
+    """The benchmark workload (perturbed Q1 128^3, K(k_e) + M + sin3 load) entry by entry
+    against the oracle: the DOF map, the pruned CSR patterns and every value."""
+    from proxpde_gb300 import meshgen
+    from proxpde_gb300._lib import ARITH_DFL, ARITH_FP64
+
+    n = 128
+    xyz, conn = meshgen.cube_hex(n)
+    xyz = meshgen.perturb(xyz, n, 0.2, 20261205)
+    k = meshgen.lognormal(20261206, conn.shape[0], 1.0)
+    ops = [{"stiffness": 2, "stiff_coef": 1.0}, {"mass": 1, "mass_coef": 1.0}]
+    rhs = {"kind": 1, "fn": O.FN_SIN3, "coef": 1.0}
+    g = gpu_assemble(O.Q1HEX, xyz, conn, ops, rhs=rhs, k=k, arith=ARITH_DFL if arith == "dfl" else ARITH_FP64)
+    em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
+    assert ndof == g["ndof"] and np.array_equal(em, g["em"])
+    nt = _threads()
+    for m, op in enumerate(ops):
+        csr, _ = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=nt)
+        compare_csr(g["mats"][m], csr, ndof, what=f"q1 128^3 {arith} {'KM'[m]}")
+        del csr
+    _, b = O.build(O.Q1HEX, xyz, conn, em, ndof, rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0}, nthreads=nt)
+    assert_close(g["b"], b, what=f"q1 128^3 {arith} b")
+
+
+@pytest.mark.parametrize("arith", ["fp64", "dfl"])
+def test_p2_64_entrywise(engine, arith):
+    """Perturbed P2 64^3 x 6 Kuhn tetrahedra, K(k_e) + M, entry by entry against the
+    oracle."""
+    from proxpde_gb300 import meshgen
+    from proxpde_gb300._lib import ARITH_DFL, ARITH_FP64
+
+    n = 64
+    xyz, conn = meshgen.cube_tet6(n)
+    xyz = meshgen.perturb(xyz, n, 0.15, 20261207)
+    k = meshgen.lognormal(20261208, conn.shape[0], 0.5)
+    ops = [{"stiffness": 2, "stiff_coef": 1.0}, {"mass": 1, "mass_coef": 1.0}]
+    g = gpu_assemble(O.P2TET, xyz, conn, ops, k=k, arith=ARITH_DFL if arith == "dfl" else ARITH_FP64)
+    em, ndof = O.dofmap(O.P2TET, xyz.shape[0], conn)
+    assert ndof == g["ndof"] and np.array_equal(em, g["em"])
+    nt = _threads()
+    for m, op in enumerate(ops):
+        csr, _ = O.build(O.P2TET, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=nt)
+        compare_csr(g["mats"][m], csr, ndof, what=f"p2 64^3x6 {arith} {'KM'[m]}")
+        del csr
 
 
 def test_q1_96_adjoint(engine):

@@ -1,7 +1,9 @@
 """proxpde's golden tests run end to end on the GPU engine through the Builder mirror:
-assemble on the device, solve on the host (scipy direct solve, like the reference's
-UmfPackLU), compare ||u - I_h u_exact||_2 with the pinned value (tolerance 1e-12,
-include/def.hpp:357-385)."""
+assemble on the device, solve with the mirror's LUSolver (UmfPackLU's interface over the
+device CG, to a relative residual of 1e-14), compare ||u - I_h u_exact||_2 with the
+pinned value (tolerance 1e-12, include/def.hpp:357-385).  A scipy direct solve of the
+same system is the cross-check; the Stokes systems are indefinite, which the CG does
+not take, and are solved by scipy."""
 import os
 
 import numpy as np
@@ -12,6 +14,11 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
+def poisson_rhs(p):
+    """The reference's rhs lambda (test/poisson3dhex.cpp:25-30), on the host."""
+    return 2.5 * np.pi ** 2 * np.sin(0.5 * np.pi * p[:, 0]) * np.sin(1.5 * np.pi * p[:, 1])
+
+
 def run(px, mesh, order, rhs_kind):
     fe = px.FESpace(mesh, order)
     bcs = [px.BCEss(fe, px.side.LEFT), px.BCEss(fe, px.side.BOTTOM)]
@@ -19,17 +26,25 @@ def run(px, mesh, order, rhs_kind):
     builder.buildLhs((px.AssemblyStiffness(1.0, fe),), bcs)
     if rhs_kind == "analytic":
         builder.buildRhs((px.AssemblyRhsAnalytic(px.FN_POISSON_RHS, fe),), bcs)
+    elif rhs_kind == "callable":
+        builder.buildRhs((px.AssemblyRhsAnalytic(poisson_rhs, fe),), bcs)
     else:
         proj = px.interpolateAnalyticFunction(px.FN_POISSON_RHS, fe)
         builder.buildRhs((px.AssemblyProjection(1.0, proj, fe),), bcs)
     builder.closeMatrix()
-    u = spla.spsolve(builder.A.tocsc(), builder.b)
+    solver = px.LUSolver()
+    solver.analyzePattern(builder)
+    solver.factorize(builder)
+    u = solver.solve(builder.b)
+    assert solver.rel_res <= 1e-14
     exact = px.interpolateAnalyticFunction(px.FN_POISSON_EXACT, fe)
-    return float(np.linalg.norm(u - exact))
+    ud = spla.spsolve(builder.A.tocsc(), builder.b)
+    return float(np.linalg.norm(u - exact)), float(np.linalg.norm(ud - exact))
 
 
 @pytest.mark.parametrize("elem,order,n,rhs,expected", [
     ("hex", 1, 4, "analytic", 0.1352139631934435),        # test/poisson3dhex.cpp:118
+    ("hex", 1, 4, "callable", 0.1352139631934435),        # the same with the rhs as a host function
     ("hex", 2, 4, "analytic", 0.0070042836287997),        # test/poisson3dhex_q2.cpp:120
     ("hex", 2, 8, "analytic", 0.001164556821288369),      # test/poisson3dhex_q2.cpp:126
     ("tet", 2, 4, "proj", 0.08097818482375403),           # test/poisson3dtet_p2.cpp:124
@@ -38,7 +53,9 @@ def run(px, mesh, order, rhs_kind):
 def test_golden_structured(engine, elem, order, n, rhs, expected):
     px = engine
     mesh = px.buildHyperCube(px.Hexahedron if elem == "hex" else px.Tetrahedron, n)
-    assert abs(run(px, mesh, order, rhs) - expected) < 1e-12
+    e_dev, e_host = run(px, mesh, order, rhs)
+    assert abs(e_dev - expected) < 1e-12, (e_dev, expected)
+    assert abs(e_host - expected) < 1e-12, (e_host, expected)
 
 
 def test_golden_unstructured_p1(engine):
@@ -46,7 +63,8 @@ def test_golden_unstructured_p1(engine):
     px = engine
     d = np.load(os.path.join(GOLDEN, "cube_uns.npz"))
     mesh = px.Mesh(px.Tetrahedron, d["xyz"], d["tets"], facets=(d["tris"], d["tri_tags"]))
-    assert abs(run(px, mesh, 1, "proj") - 0.88528925443) < 1e-12
+    e_dev, e_host = run(px, mesh, 1, "proj")
+    assert abs(e_dev - 0.88528925443) < 1e-12 and abs(e_host - 0.88528925443) < 1e-12, (e_dev, e_host)
 
 
 @pytest.mark.parametrize("elem,expected", [

@@ -9,6 +9,7 @@ import pytest
 
 import oracle as O
 from helpers import assert_close, compare_csr, gpu_assemble, oracle_lhs, problem, structural_pattern
+from proxpde_gb300._lib import ARITH_DFL, ARITH_FP64
 
 pytestmark = pytest.mark.gpu
 
@@ -27,7 +28,7 @@ CASES = [
     ("q1_mixed_op", O.Q1HEX, "hex", 5, 0.2, 1.0, [{"stiffness": 2, "stiff_coef": 0.5, "mass": 1, "mass_coef": 3.0}],
      None),
     # unperturbed hexahedra, k = 1: the face-neighbour stiffness entries cancel exactly,
-    # so the prune step sees round-off residues of the double-float arithmetic
+    # so the prune step sees round-off residues
     ("q1hex_uniform_12", O.Q1HEX, "hex", 12, 0.0, None, [K1_OP, M_OP], {"kind": 1, "fn": O.FN_SIN3, "coef": 1.0}),
 ]
 
@@ -42,12 +43,21 @@ def test_parity(engine, case):
     assert np.array_equal(g["em"], em), "first-touch DOF map differs"
     rp_s, ci_s = structural_pattern(em, ndof)
     assert np.array_equal(g["pattern"][0], rp_s) and np.array_equal(g["pattern"][1], ci_s)
-    for op, mat in zip(ops, g["mats"]):
+    for m, (op, mat) in enumerate(zip(ops, g["mats"])):
         csr, _ = O.build(t, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=4)
-        compare_csr(mat, csr, ndof)
+        # the pruned pattern is bit-exact: no entry kept on one side only
+        assert compare_csr(mat, csr, ndof, what=f"parity {case[0]} op{m}") == 0
+        # entries near the prune threshold were recomputed in the reference's order:
+        # bit for bit the oracle's values
+        rows = np.repeat(np.arange(ndof), np.diff(csr[0]))
+        rowmax = np.zeros(ndof)
+        np.maximum.at(rowmax, rows, np.abs(csr[2]))
+        near = np.abs(csr[2]) <= 1e-16 + 16 * 2.220446049250313e-16 * rowmax[rows]
+        if near.any():
+            assert np.array_equal(mat[2][near], csr[2][near])
     if rhs is not None:
         _, b = O.build(t, xyz, conn, em, ndof, rhs={"kind": rhs["kind"], "fn": rhs["fn"], "c": rhs["coef"]})
-        assert_close(g["b"], b, what="rhs")
+        assert_close(g["b"], b, what=f"parity {case[0]} rhs")
 
 
 def test_prune_cancellation_margin(engine):
@@ -170,19 +180,29 @@ def test_invalid_inputs_rejected(engine):
     assert torch.isfinite(v).all()
 
 
-@pytest.mark.parametrize("kernel", ["dfl", "fp64", "thread-dfl", "thread-fp64", "generic"])
+Q1_KERNELS = ["fp64", "group-dfl", "group-fp64", "thread-dfl", "thread-fp64", "generic"]
+
+
+def q1_kernel(monkeypatch, kernel):
+    """Select a Q1 kernel for the contexts created next; returns its arithmetic."""
+    monkeypatch.setenv("PXG_Q1_GENERIC", "1" if kernel == "generic" else "0")
+    monkeypatch.setenv("PXG_Q1_THREAD", "1" if kernel.startswith("thread") else "0")
+    monkeypatch.setenv("PXG_Q1_GROUP", "1" if kernel.startswith("group") else "0")
+    return ARITH_DFL if kernel.endswith("dfl") else ARITH_FP64
+
+
+@pytest.mark.parametrize("kernel", Q1_KERNELS)
 @pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
 @pytest.mark.parametrize("n", [7, 40])
 def test_q1_kernels_agree_with_oracle(engine, monkeypatch, kernel, bc, n):
-    """The Q1 kernels against the oracle: the eight-lanes-per-element tensor-product
-    kernel in double-float arithmetic (default) and in FP64, the one-thread-per-element
-    kernel in both arithmetics, and the generic kernel; K(k_e) + M + sin3 load on a
-    perturbed mesh, with and without inhomogeneous Dirichlet data.  n = 40 takes the
-    short-series path of the load (small offsets), n = 7 the direct sinpi path; 7^3
-    elements also leave a partly filled last block."""
-    monkeypatch.setenv("PXG_Q1_GENERIC", "1" if kernel == "generic" else "0")
-    monkeypatch.setenv("PXG_Q1_FP64", "1" if kernel.endswith("fp64") else "0")
-    monkeypatch.setenv("PXG_Q1_THREAD", "1" if kernel.startswith("thread") else "0")
+    """The Q1 kernels against the oracle: the FP64 one-thread-per-element kernel
+    (default), the eight-lanes-per-element tensor-product kernel and the older
+    one-thread tensor-product kernel, each in double-float and in FP64, and the generic
+    per-quadrature-point kernel; K(k_e) + M + sin3 load on a perturbed mesh, with and
+    without inhomogeneous Dirichlet data.  n = 40 takes the short-series path of the
+    load (small offsets), n = 7 the direct sinpi path; 7^3 elements also leave a partly
+    filled last block."""
+    arith = q1_kernel(monkeypatch, kernel)
     xyz, conn, k = problem("hex", n, 0.2, seed=21, sigma=1.0)
     em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
     bcarg, mask, val = None, None, None
@@ -196,27 +216,29 @@ def test_q1_kernels_agree_with_oracle(engine, monkeypatch, kernel, bc, n):
         bcarg = (dofs, val[dofs])
         ops[0]["apply_bc"] = 1
         rhs["apply_bc"] = 1
-    g = gpu_assemble(O.Q1HEX, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg)
+    g = gpu_assemble(O.Q1HEX, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg, arith=arith)
     csrK, b = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs=oracle_lhs(ops[0], k), bc_mask=mask, bc_val=val)
     csrM, _ = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs=oracle_lhs(ops[1], k))
     _, b = O.build(O.Q1HEX, xyz, conn, em, ndof, rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0, "apply_bc": int(bc)},
                    bc_mask=mask, bc_val=val, b=b)
-    compare_csr(g["mats"][0], csrK, ndof)
-    compare_csr(g["mats"][1], csrM, ndof)
-    assert_close(g["b"], b, what="rhs")
+    compare_csr(g["mats"][0], csrK, ndof, what=f"q1 {kernel} K")
+    compare_csr(g["mats"][1], csrM, ndof, what=f"q1 {kernel} M")
+    assert_close(g["b"], b, what=f"q1 {kernel} b")
 
 
-@pytest.mark.parametrize("kernel", ["dfl", "fp64"])
+@pytest.mark.parametrize("kernel", ["fp64", "dfl", "generic"])
 @pytest.mark.parametrize("t,gen,n", [(O.P1TET, "tet6", 9), (O.P2TET, "tet6", 5), (O.P2TET, "tet5", 4)],
                          ids=["p1tet6", "p2tet6", "p2tet5"])
 @pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
 @pytest.mark.parametrize("rhs_fn", ["const", "sin3"])
 def test_tet_kernels_agree_with_oracle(engine, monkeypatch, kernel, t, gen, n, bc, rhs_fn):
-    """The tetrahedron kernels against the oracle: double-float entries (default) and
-    FP64 (PXG_TET_FP64=1); K(k_e) + M with a load (the constant load takes the
-    closed-form path of the double-float kernel), with and without inhomogeneous
-    Dirichlet data."""
-    monkeypatch.setenv("PXG_TET_FP64", "1" if kernel == "fp64" else "0")
+    """The tetrahedron kernels against the oracle: reference-tensor entries in FP64
+    (default) and in double-float, and the per-quadrature-point FP64 kernel
+    (PXG_TET_GENERIC=1); K(k_e) + M with a load (the constant load takes the closed-form
+    path of the reference-tensor kernels), with and without inhomogeneous Dirichlet
+    data."""
+    monkeypatch.setenv("PXG_TET_GENERIC", "1" if kernel == "generic" else "0")
+    arith = ARITH_DFL if kernel == "dfl" else ARITH_FP64
     xyz, conn, k = problem(gen, n, 0.15, seed=23, sigma=0.5)
     em, ndof = O.dofmap(t, xyz.shape[0], conn)
     fn = O.FN_CONST if rhs_fn == "const" else O.FN_SIN3
@@ -231,30 +253,35 @@ def test_tet_kernels_agree_with_oracle(engine, monkeypatch, kernel, t, gen, n, b
         bcarg = (dofs, val[dofs])
         ops[0]["apply_bc"] = 1
         rhs["apply_bc"] = 1
-    g = gpu_assemble(t, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg)
+    g = gpu_assemble(t, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg, arith=arith)
     csrK, b = O.build(t, xyz, conn, em, ndof, lhs=oracle_lhs(ops[0], k), bc_mask=mask, bc_val=val)
     csrM, _ = O.build(t, xyz, conn, em, ndof, lhs=oracle_lhs(ops[1], k))
     _, b = O.build(t, xyz, conn, em, ndof, rhs={"kind": 1, "fn": fn, "c": 2.0, "apply_bc": int(bc)},
                    bc_mask=mask, bc_val=val, b=b)
-    compare_csr(g["mats"][0], csrK, ndof)
-    compare_csr(g["mats"][1], csrM, ndof)
-    assert_close(g["b"], b, what="rhs")
+    name = O.NAMES[t]
+    compare_csr(g["mats"][0], csrK, ndof, what=f"{name} {kernel} K")
+    compare_csr(g["mats"][1], csrM, ndof, what=f"{name} {kernel} M")
+    assert_close(g["b"], b, what=f"{name} {kernel} b")
 
 
-MASS_FE_KERNELS = [(O.P1TET, "tet6", 5, {}), (O.P2TET, "tet6", 3, {}), (O.P2TET, "tet6", 3, {"PXG_TET_FP64": "1"}),
-                   (O.Q1HEX, "hex", 5, {}), (O.Q1HEX, "hex", 5, {"PXG_Q1_THREAD": "1"}),
-                   (O.Q1HEX, "hex", 4, {"PXG_Q1_GENERIC": "1"}), (O.Q2HEX, "hex", 3, {}),
-                   (O.Q2HEX, "hex", 2, {"PXG_Q2_FP64": "1"})]
+MASS_FE_KERNELS = [(O.P1TET, "tet6", 5, {}, ARITH_FP64), (O.P1TET, "tet6", 5, {}, ARITH_DFL),
+                   (O.P2TET, "tet6", 3, {}, ARITH_FP64), (O.P2TET, "tet6", 3, {}, ARITH_DFL),
+                   (O.P2TET, "tet6", 3, {"PXG_TET_GENERIC": "1"}, ARITH_FP64),
+                   (O.Q1HEX, "hex", 5, {}, ARITH_FP64), (O.Q1HEX, "hex", 5, {}, ARITH_DFL),
+                   (O.Q1HEX, "hex", 5, {"PXG_Q1_THREAD": "1"}, ARITH_DFL),
+                   (O.Q1HEX, "hex", 4, {"PXG_Q1_GENERIC": "1"}, ARITH_FP64), (O.Q2HEX, "hex", 2, {}, ARITH_FP64),
+                   (O.Q2HEX, "hex", 3, {}, ARITH_DFL)]
+MASS_FE_IDS = ["p1", "p1_dfl", "p2", "p2_dfl", "p2_generic", "q1", "q1_group_dfl", "q1_thread_dfl", "q1_generic",
+               "q2", "q2_dfl"]
 
 
-@pytest.mark.parametrize("t,gen,n,env", MASS_FE_KERNELS,
-                         ids=["p1", "p2", "p2_fp64", "q1", "q1_thread", "q1_generic", "q2", "q2_fp64"])
-def test_mass_fe_coefficient_matches_oracle(engine, monkeypatch, t, gen, n, env):
+@pytest.mark.parametrize("t,gen,n,env,arith", MASS_FE_KERNELS, ids=MASS_FE_IDS)
+def test_mass_fe_coefficient_matches_oracle(engine, monkeypatch, t, gen, n, env, arith):
     """AssemblyMassFE with the per-element coefficient (mass kind 2, times mass_coef)
     in every element kernel against the oracle: alone (the mass coefficient folded
     where a kernel folds a single operator's), beside AssemblyStiffnessFE on the same
     coefficient, and in one operator with a constant stiffness, with Dirichlet data."""
-    for v in ("PXG_TET_FP64", "PXG_Q1_THREAD", "PXG_Q1_GENERIC", "PXG_Q2_FP64"):
+    for v in ("PXG_TET_GENERIC", "PXG_Q1_THREAD", "PXG_Q1_GENERIC", "PXG_Q1_GROUP", "PXG_Q2_GENERIC"):
         monkeypatch.setenv(v, env.get(v, "0"))
     xyz, conn, k = problem(gen, n, 0.15, seed=29, sigma=1.0)
     em, ndof = O.dofmap(t, xyz.shape[0], conn)
@@ -266,27 +293,27 @@ def test_mass_fe_coefficient_matches_oracle(engine, monkeypatch, t, gen, n, env)
                 [{"stiffness": 2, "stiff_coef": 1.0}, {"mass": 2, "mass_coef": 2.0}],
                 [{"stiffness": 1, "stiff_coef": 0.5, "mass": 2, "mass_coef": 3.0, "apply_bc": 1}]):
         bc = (dofs, val[dofs]) if any(o.get("apply_bc") for o in ops) else None
-        g = gpu_assemble(t, xyz, conn, ops, k=k, bc=bc)
+        g = gpu_assemble(t, xyz, conn, ops, k=k, bc=bc, arith=arith)
         for op, mat in zip(ops, g["mats"]):
             o = oracle_lhs(op, k)
             kw = dict(bc_mask=mask, bc_val=val) if op.get("apply_bc") else {}
             csr, b = O.build(t, xyz, conn, em, ndof, lhs=o, **kw)
-            compare_csr(mat, csr, ndof)
+            compare_csr(mat, csr, ndof, what=f"massFE {O.NAMES[t]} {env} arith{arith}")
             if op.get("apply_bc"):
                 assert_close(g["b"], b, what="lift")
 
 
-@pytest.mark.parametrize("kernel", ["dfl", "fp64"])
+@pytest.mark.parametrize("kernel", ["fp64", "group-dfl", "group-fp64"])
 def test_q1_two_stiffness_operators(engine, monkeypatch, kernel):
-    """The Q1 group kernel with two stiffness operators of different coefficients, one
-    of them combined with a mass term of coefficient 2, and with the operators swapped
+    """The Q1 kernels with two stiffness operators of different coefficients, one of
+    them combined with a mass term of coefficient 2, and with the operators swapped
     (mass first), on a perturbed mesh with a partly filled last block."""
-    monkeypatch.setenv("PXG_Q1_FP64", "1" if kernel == "fp64" else "0")
+    arith = q1_kernel(monkeypatch, kernel)
     xyz, conn, k = problem("hex", 7, 0.2, seed=37, sigma=1.0)
     em, ndof = O.dofmap(O.Q1HEX, xyz.shape[0], conn)
     for ops in ([{"stiffness": 2, "stiff_coef": 0.75, "mass": 1, "mass_coef": 2.0}, {"stiffness": 1, "stiff_coef": 3.0}],
                 [{"mass": 1, "mass_coef": 0.3}, {"stiffness": 2, "stiff_coef": 2.5}]):
-        g = gpu_assemble(O.Q1HEX, xyz, conn, ops, k=k)
+        g = gpu_assemble(O.Q1HEX, xyz, conn, ops, k=k, arith=arith)
         for op, mat in zip(ops, g["mats"]):
             csr, _ = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs=oracle_lhs(op, k))
             compare_csr(mat, csr, ndof)
@@ -304,16 +331,17 @@ def test_tet_two_stiffness_operators(engine):
         compare_csr(mat, csr, ndof)
 
 
-@pytest.mark.parametrize("kernel", ["dfl", "fp64"])
+@pytest.mark.parametrize("kernel", ["fp64", "dfl"])
 @pytest.mark.parametrize("n", [3, 5])
 @pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
 @pytest.mark.parametrize("rhs_kind", ["sin3", "projection"])
 def test_q2_kernels_agree_with_oracle(engine, monkeypatch, kernel, n, bc, rhs_kind):
-    """The Q2 kernels against the oracle: the block-per-element double-float kernel
-    (default) and the FP64 element kernel (PXG_Q2_FP64=1); K(k_e) + M with an analytic
-    or a projected load, with and without inhomogeneous Dirichlet data; n = 5 gives
-    more elements than the persistent grid has blocks only on small GPUs, n = 3 fewer."""
-    monkeypatch.setenv("PXG_Q2_FP64", "1" if kernel == "fp64" else "0")
+    """The Q2 kernels against the oracle: the FP64 element kernel (default) and the
+    block-per-element double-float kernel; K(k_e) + M with an analytic or a projected
+    load, with and without inhomogeneous Dirichlet data; n = 5 gives more elements than
+    the persistent grid of the double-float kernel has blocks only on small GPUs, n = 3
+    fewer."""
+    arith = ARITH_DFL if kernel == "dfl" else ARITH_FP64
     xyz, conn, k = problem("hex", n, 0.2, seed=31, sigma=1.0)
     em, ndof = O.dofmap(O.Q2HEX, xyz.shape[0], conn)
     dx = O.dof_coords(O.Q2HEX, xyz, conn, em, ndof)
@@ -334,13 +362,13 @@ def test_q2_kernels_agree_with_oracle(engine, monkeypatch, kernel, n, bc, rhs_ki
         ops[0]["apply_bc"] = 1
         rhs["apply_bc"] = 1
         orhs["apply_bc"] = 1
-    g = gpu_assemble(O.Q2HEX, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg, field=field)
+    g = gpu_assemble(O.Q2HEX, xyz, conn, ops, rhs=rhs, k=k, bc=bcarg, field=field, arith=arith)
     csrK, b = O.build(O.Q2HEX, xyz, conn, em, ndof, lhs=oracle_lhs(ops[0], k), bc_mask=mask, bc_val=val)
     csrM, _ = O.build(O.Q2HEX, xyz, conn, em, ndof, lhs=oracle_lhs(ops[1], k))
     _, b = O.build(O.Q2HEX, xyz, conn, em, ndof, rhs=orhs, bc_mask=mask, bc_val=val, b=b)
-    compare_csr(g["mats"][0], csrK, ndof)
-    compare_csr(g["mats"][1], csrM, ndof)
-    assert_close(g["b"], b, what="rhs")
+    compare_csr(g["mats"][0], csrK, ndof, what=f"q2 {kernel} K")
+    compare_csr(g["mats"][1], csrM, ndof, what=f"q2 {kernel} M")
+    assert_close(g["b"], b, what=f"q2 {kernel} b")
 
 
 def test_q2_two_stiffness_operators(engine):

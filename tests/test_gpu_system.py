@@ -156,3 +156,47 @@ def test_vector_loads_match_oracle(engine, elem):
     pq = px.FESpace(mesh, 1, offset=0, qr_order=2)
     with pytest.raises(px.PxgError):
         px.Builder(ndp).buildRhs((px.AssemblyRhsAnalytic(px.FN_CONST, pq),))  # loads use the element's rule
+
+
+def test_system_close_above_noalloc_cap(engine):
+    """pxg_sys_close_matrix (the system Builder's closeMatrix) has no row limit and no
+    shared scratch: a 3-component P1 space with more rows than the allocation-free
+    prune's 4,194,304, mass only (the component-cross blocks are structural zeros
+    that the prune removes), matches the host-side prune of the same values, and two
+    systems close one after the other on one stream with their own results."""
+    import torch
+
+    from proxpde_gb300 import Context, meshgen
+    from proxpde_gb300._lib import OP_MASS, System
+
+    xyz, conn = meshgen.cube_tet6(112)
+    c = Context(0)
+    c.set_mesh(O.P1TET, xyz, conn)
+    nd = c.build_dofmap()
+    S = System([c], [3])
+    assert S.ntot == 3 * nd > 4_194_304
+    vals = torch.zeros(S.nnz, dtype=torch.float64, device="cuda")
+    S.assemble(0, 0, [(OP_MASS, 1.0)], vals)
+    rp = torch.empty(S.ntot + 1, dtype=torch.int32, device="cuda")
+    ci = torch.empty(S.nnz, dtype=torch.int32, device="cuda")
+    vo = torch.empty(S.nnz, dtype=torch.float64, device="cuda")
+    kept = S.close_matrix(vals, rp, ci, vo)
+    torch.cuda.synchronize()
+    A = device_closed(S, vals)
+    assert kept == A.nnz and kept * 3 == S.nnz  # one block of three per row survives
+    assert np.array_equal(rp.cpu().numpy(), A.indptr)
+    assert np.array_equal(ci[:kept].cpu().numpy(), A.indices)
+    assert np.array_equal(vo[:kept].cpu().numpy(), A.data)
+    # a second, smaller system closed right after on the same stream keeps its own counts
+    xyz2, conn2 = meshgen.cube_tet6(4)
+    c2 = Context(0)
+    c2.set_mesh(O.P1TET, xyz2, conn2)
+    c2.build_dofmap()
+    S2 = System([c2], [2])
+    v2 = torch.zeros(S2.nnz, dtype=torch.float64, device="cuda")
+    S2.assemble(0, 0, [(OP_MASS, 1.0)], v2)
+    rp2 = torch.empty(S2.ntot + 1, dtype=torch.int32, device="cuda")
+    ci2 = torch.empty(S2.nnz, dtype=torch.int32, device="cuda")
+    vo2 = torch.empty(S2.nnz, dtype=torch.float64, device="cuda")
+    assert S2.close_matrix(v2, rp2, ci2, vo2) * 2 == S2.nnz
+    assert S.close_matrix(vals, rp, ci, vo) == kept

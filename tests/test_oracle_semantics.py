@@ -164,3 +164,20 @@ def test_mass_fe_coefficient(oracle_lib, t, gen):
         Me, _ = O.element(t, xyz, conn, e, lhs={"mass_kind": 2, "m_e": k})
         M1, _ = O.element(t, xyz, conn, e, lhs={"mass_kind": 1, "mass_c": 1.0})
         assert np.allclose(Me, k[e] * M1, rtol=1e-15, atol=0.0)
+
+
+@pytest.mark.parametrize("t,gen", [(O.P1TET, "tet6"), (O.P2TET, "tet5"), (O.Q1HEX, "hex"), (O.Q2HEX, "hex")])
+def test_values_at_qpoints_reproduce_analytic_load(t, gen):
+    """rhs kind 3 (values at CurFE::qpoint, evaluated by the caller) reproduces
+    AssemblyRhsAnalytic of the same function evaluated inside the oracle (kind 1):
+    the points are the reference's qpoint = origin + J xi (curfe.hpp:80)."""
+    from proxpde_gb300 import meshgen
+
+    xyz, conn = {"tet6": meshgen.cube_tet6, "tet5": meshgen.cube_tet5, "hex": meshgen.cube_hex}[gen](3)
+    xyz = meshgen.perturb(xyz, 3, 0.15, 47)
+    em, nd = O.dofmap(t, xyz.shape[0], conn)
+    qp = O.qpoints(t, xyz, conn).reshape(-1, 3)
+    v = np.sin(np.pi * qp[:, 0]) * np.sin(np.pi * qp[:, 1]) * np.sin(np.pi * qp[:, 2])
+    _, b3 = O.build(t, xyz, conn, em, nd, rhs={"kind": 3, "c": 2.0, "field": v})
+    _, b1 = O.build(t, xyz, conn, em, nd, rhs={"kind": 1, "fn": O.FN_SIN3, "c": 2.0})
+    assert np.abs(b3 - b1).max() <= 1e-15 * np.abs(b1).max()

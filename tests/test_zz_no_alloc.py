@@ -64,3 +64,62 @@ def test_noalloc_rejects_oversize(engine):
     n_out = C.c_int64(-1)
     st = L.pxg_prune_csr_noalloc(1, 1, 1, (1 << 22) + 1, 1, 1, 1, C.byref(n_out), None)
     assert st == 1 and n_out.value == -1
+
+
+@pytest.mark.parametrize("nrows", [5_000, 1 << 22], ids=["5k", "max"])
+def test_noalloc_ragged_csr_and_no_allocation(engine, nrows):
+    """A ragged synthetic CSR (empty rows included; values of both signs, exact zeros,
+    1e-17, exactly 1e-16 and just above it) with more rows than one block-total scan
+    thread covers, up to the 4,194,304-row maximum, against numpy's prune; and the
+    call allocates no device memory: torch's allocator and the device's free memory
+    (cudaMemGetInfo) are unchanged across it, after a first call that sets up the
+    scratch address."""
+    import torch
+
+    from proxpde_gb300 import _lib
+
+    rng = np.random.default_rng(nrows)
+    lens = rng.integers(0, 5 if nrows > 100_000 else 17, nrows)
+    lens[rng.random(nrows) < 0.05] = 0
+    rp = np.zeros(nrows + 1, dtype=np.int32)
+    np.cumsum(lens, out=rp[1:])
+    nnz = int(rp[-1])
+    ci = rng.integers(0, nrows, nnz).astype(np.int32)
+    vals = rng.standard_normal(nnz)
+    pick = rng.random(nnz)
+    vals[pick < 0.2] = 0.0
+    vals[(pick >= 0.2) & (pick < 0.25)] = 1e-17
+    vals[(pick >= 0.25) & (pick < 0.28)] = -1e-16
+    vals[(pick >= 0.28) & (pick < 0.31)] = 1.0000001e-16
+    keep = ~(np.abs(vals) <= 1e-16)
+    rows = np.repeat(np.arange(nrows), lens)
+    kept_rows = np.bincount(rows[keep], minlength=nrows)
+    rp_ref = np.zeros(nrows + 1, dtype=np.int32)
+    np.cumsum(kept_rows, out=rp_ref[1:])
+    m = int(keep.sum())
+
+    d_rp, d_ci, d_v = (torch.as_tensor(x).cuda() for x in (rp, ci, vals))
+    out_rp = torch.empty(nrows + 1, dtype=torch.int32, device="cuda")
+    out_ci = torch.empty(nnz, dtype=torch.int32, device="cuda")
+    out_v = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    L = _lib.load()
+
+    def call():
+        n_out = C.c_int64(-1)
+        st = L.pxg_prune_csr_noalloc(d_rp.data_ptr(), d_ci.data_ptr(), d_v.data_ptr(), nrows, out_rp.data_ptr(),
+                                     out_ci.data_ptr(), out_v.data_ptr(), C.byref(n_out), None)
+        assert st == 0
+        return n_out.value
+
+    assert call() == m
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_allocated()
+    assert call() == m
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert torch.cuda.memory_allocated() == alloc0
+    assert free1 == free0, (free0, free1)
+    assert np.array_equal(out_rp.cpu().numpy(), rp_ref)
+    assert np.array_equal(out_ci[:m].cpu().numpy(), ci[keep])
+    assert np.array_equal(out_v[:m].cpu().numpy(), vals[keep])
