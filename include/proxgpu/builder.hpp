@@ -1024,12 +1024,19 @@ struct Builder<void, Storage>
         }
         check(pxg_set_bc(sp.ctx, d.data(), v.data(), (int64_t)d.size(), diag, PXG_MEM_HOST), sp.ctx, "pxg_set_bc");
         DeviceArray<double> f;
-        size_t const fn = part.kind == 3 ? (size_t)sp.nelem * sp.nq : (size_t)sp.ndof;
-        size_t const foff = part.kind == 3 ? 0 : (size_t)part.fieldComp * sp.ndof;
-        if (part.field)
-          f = DeviceArray<double>(sp.ctx, fn);
-        if (part.field)
-          check(pxg_memcpy(sp.ctx, f.p, part.field + foff, fn * sizeof(double), 0, nullptr), sp.ctx, "pxg_memcpy");
+        if (part.kind == 3)
+        {
+          f = DeviceArray<double>(sp.ctx, part.qvals.size());
+          check(pxg_memcpy(sp.ctx, f.p, part.qvals.data(), part.qvals.size() * sizeof(double), 0, nullptr), sp.ctx,
+                "pxg_memcpy");
+        }
+        else if (part.field)
+        {
+          f = DeviceArray<double>(sp.ctx, (size_t)sp.ndof);
+          check(pxg_memcpy(sp.ctx, f.p, part.field + (size_t)part.fieldComp * sp.ndof, (size_t)sp.ndof * sizeof(double),
+                           0, nullptr),
+                sp.ctx, "pxg_memcpy");
+        }
         pxg_rhs_op op{part.kind, part.fn, part.coef, f.p, r.bcs.empty() ? 0 : 1};
         check(pxg_assemble(sp.ctx, nullptr, nullptr, nullptr, nullptr, &op, bd.p + sp.offset + lo, PXG_ACCUMULATE,
                            nullptr),
@@ -1059,8 +1066,6 @@ private:
     pxg_ctx * ctx;
     int dim, qr;
     int64_t offset, ndof;
-    int64_t nelem;
-    int nq; // quadrature points per element of the element type's own rule
   };
   struct Call
   {
@@ -1073,8 +1078,9 @@ private:
   {
     int block, kind, fn;
     double coef;
-    double const * field; // projection: the whole field on the host; kind 3: the values
-    int fieldComp;        // at the quadrature points; else null
+    double const * field; // projection: the whole field on the host, else null
+    int fieldComp;
+    std::vector<double> qvals; // kind 3: a copy of the values at the quadrature points
   };
   struct RhsCall
   {
@@ -1098,11 +1104,13 @@ private:
   {
     checkRule<X>();
     RhsCall r{spaceOf(*a.feSpace), {}, bcs};
+    // the calls run at closeMatrix: the parts keep what they need (the assembly object
+    // may be a temporary of the buildRhs call)
     for (int c: a.comps)
       if (a.qvals.empty())
-        r.parts.push_back(RhsPart{c, 1, a.fns[(size_t)c], a.coefs[(size_t)c], nullptr, 0});
+        r.parts.push_back(RhsPart{c, 1, a.fns[(size_t)c], a.coefs[(size_t)c], nullptr, 0, {}});
       else
-        r.parts.push_back(RhsPart{c, 3, 0, a.coefs[(size_t)c], a.qvals[(size_t)c].data(), c});
+        r.parts.push_back(RhsPart{c, 3, 0, a.coefs[(size_t)c], nullptr, c, a.qvals[(size_t)c]});
     rhsCalls.push_back(std::move(r));
   }
   template <typename X>
@@ -1111,7 +1119,7 @@ private:
     checkRule<X>();
     RhsCall r{spaceOf(*a.feSpace), {}, bcs};
     for (size_t j = 0; j < a.comps.size(); ++j)
-      r.parts.push_back(RhsPart{(int)j, 2, 0, a.coef, a.field->data(), a.comps[j]});
+      r.parts.push_back(RhsPart{(int)j, 2, 0, a.coef, a.field->data(), a.comps[j], {}});
     rhsCalls.push_back(std::move(r));
   }
 
@@ -1121,8 +1129,7 @@ private:
     for (size_t k = 0; k < spaces.size(); ++k)
       if (spaces[k].ctx == fe.ctx)
         return (int)k;
-    int const nq = FE::elemType == PXG_P1TET ? 4 : FE::elemType == PXG_P2TET ? 11 : FE::elemType == PXG_Q1HEX ? 8 : 27;
-    spaces.push_back(Space{fe.ctx, FE::dim, FE::qrType, fe.offset, fe.dof.size, fe.nelem, nq});
+    spaces.push_back(Space{fe.ctx, FE::dim, FE::qrType, fe.offset, fe.dof.size});
     return (int)spaces.size() - 1;
   }
   template <typename FE>

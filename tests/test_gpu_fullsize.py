@@ -25,7 +25,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import assert_close, compare_csr, gpu_assemble, nnz_p2_kuhn6, nnz_q1_cube, oracle_lhs, q1_quadrature
+from helpers import (EPS, EPS_DFL, assert_close, compare_csr, gpu_assemble, nnz_p2_kuhn6, nnz_q1_cube, oracle_lhs,
+                     q1_quadrature)
 
 pytestmark = pytest.mark.gpu
 
@@ -178,10 +179,10 @@ def test_q1_128_entrywise(engine, arith):
     nt = _threads()
     for m, op in enumerate(ops):
         csr, _ = O.build(O.Q1HEX, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=nt)
-        compare_csr(g["mats"][m], csr, ndof, what=f"q1 128^3 {arith} {'KM'[m]}")
+        compare_csr(g["mats"][m], csr, ndof, what=f"q1 128^3 {arith} {'KM'[m]}", eps=EPS_DFL if arith == "dfl" else EPS)
         del csr
     _, b = O.build(O.Q1HEX, xyz, conn, em, ndof, rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0}, nthreads=nt)
-    assert_close(g["b"], b, what=f"q1 128^3 {arith} b")
+    assert_close(g["b"], b, what=f"q1 128^3 {arith} b", eps=EPS_DFL if arith == "dfl" else EPS)
 
 
 @pytest.mark.parametrize("arith", ["fp64", "dfl"])
@@ -202,7 +203,7 @@ def test_p2_64_entrywise(engine, arith):
     nt = _threads()
     for m, op in enumerate(ops):
         csr, _ = O.build(O.P2TET, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=nt)
-        compare_csr(g["mats"][m], csr, ndof, what=f"p2 64^3x6 {arith} {'KM'[m]}")
+        compare_csr(g["mats"][m], csr, ndof, what=f"p2 64^3x6 {arith} {'KM'[m]}", eps=EPS_DFL if arith == "dfl" else EPS)
         del csr
 
 

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import assert_close, compare_csr, gpu_assemble, oracle_lhs, problem
+from helpers import EPS, EPS_DFL, assert_close, compare_csr, gpu_assemble, oracle_lhs, problem
 
 pytestmark = pytest.mark.gpu
 
@@ -18,13 +18,13 @@ TYPES = [(O.P1TET, "tet6", 6), (O.P2TET, "tet5", 4), (O.Q1HEX, "hex", 7), (O.Q2H
 IDS = ["p1tet", "p2tet", "q1hex", "q2hex"]
 
 
-def check_against_oracle(t, xyz, conn, k, g):
+def check_against_oracle(t, xyz, conn, k, g, eps=EPS):
     em, ndof = O.dofmap(t, xyz.shape[0], conn)
     for op, mat in zip([K_OP, M_OP], g["mats"]):
         csr, _ = O.build(t, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=4)
-        compare_csr(mat, csr, ndof)
+        compare_csr(mat, csr, ndof, eps=eps)
     _, b = O.build(t, xyz, conn, em, ndof, rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0})
-    assert_close(g["b"], b, what="rhs")
+    assert_close(g["b"], b, what="rhs", eps=eps)
 
 
 @pytest.mark.parametrize("t,gen,n", TYPES, ids=IDS)
@@ -60,15 +60,21 @@ def test_colour_scatter_matches_oracle_and_is_reproducible(engine, t, gen, n):
     assert np.array_equal(g1["b"].view(np.uint64), g2["b"].view(np.uint64))
 
 
-@pytest.mark.parametrize("t,gen,n,threads", [(O.P1TET, "tet6", 6, 64), (O.P1TET, "tet6", 6, 256),
-                                             (O.P2TET, "tet5", 4, 64), (O.P2TET, "tet5", 4, 256),
-                                             (O.Q1HEX, "hex", 7, 256), (O.Q1HEX, "hex", 7, 512)])
-def test_block_size_variants_match_oracle(engine, t, gen, n, threads):
+@pytest.mark.parametrize("t,gen,n,threads,dfl", [(O.P1TET, "tet6", 6, 64, False), (O.P1TET, "tet6", 6, 256, False),
+                                                 (O.P2TET, "tet5", 4, 64, False), (O.P2TET, "tet5", 4, 256, False),
+                                                 (O.P2TET, "tet5", 4, 256, True),
+                                                 (O.Q1HEX, "hex", 7, 64, False), (O.Q1HEX, "hex", 7, 128, False),
+                                                 (O.Q1HEX, "hex", 7, 256, True), (O.Q1HEX, "hex", 7, 512, True)])
+def test_block_size_variants_match_oracle(engine, t, gen, n, threads, dfl):
+    """Every block size of the FP64 element kernels (and of the double-float ones,
+    whose Q1 kernel has eight lanes per element) against the oracle."""
     from proxpde_gb300 import SCATTER_REDUCE
+    from proxpde_gb300._lib import ARITH_DFL, ARITH_FP64
 
     xyz, conn, k = problem(gen, n, 0.15, seed=9, sigma=1.0)
-    g = gpu_assemble(t, xyz, conn, [K_OP, M_OP], rhs=SIN3, k=k, scatter=SCATTER_REDUCE, threads=threads)
-    check_against_oracle(t, xyz, conn, k, g)
+    g = gpu_assemble(t, xyz, conn, [K_OP, M_OP], rhs=SIN3, k=k, scatter=SCATTER_REDUCE, threads=threads,
+                     arith=ARITH_DFL if dfl else ARITH_FP64)
+    check_against_oracle(t, xyz, conn, k, g, eps=EPS_DFL if dfl else EPS)
 
 
 def test_bad_block_size_is_rejected(engine):
