@@ -991,6 +991,23 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
 // constant memory), the mass entry |det J| Mhat_ij (a single mass operator's
 // coefficient folded into |det J|).  About 450 FP64 operations per P2 element
 // against about 1,000 for the per-quadrature-point form of kAssemble.
+// P2 tetrahedron (src/reffe.cpp:542-642, vertices then the edges 01 12 20 03 13 23):
+// bit a of the mask is set where d/dx_a phi_i is not identically zero (phi_1 depends
+// on x only, phi_5 = 4xy on x and y, ...).  A reference-tensor term whose derivative is
+// identically zero is an exact zero in the table, so skipping it changes no value.
+__host__ __device__ constexpr unsigned p2GradMask(int i)
+{
+  return i == 1 ? 1u : i == 2 ? 2u : i == 3 ? 4u : i == 5 ? 3u : i == 8 ? 5u : i == 9 ? 6u : 7u;
+}
+// term k (xx yy zz xy xz yz) of entry (i, j) of the P2 reference tensor can be nonzero
+__host__ __device__ constexpr bool p2Term(int k, int i, int j)
+{
+  int const a = k < 3 ? k : (k == 5 ? 1 : 0), b = k < 3 ? k : (k == 3 ? 1 : 2);
+  bool const ab = ((p2GradMask(i) >> a) & 1u) && ((p2GradMask(j) >> b) & 1u);
+  bool const ba = ((p2GradMask(i) >> b) & 1u) && ((p2GradMask(j) >> a) & 1u);
+  return k < 3 ? ab : (ab || ba);
+}
+
 template <int T, int NT>
 __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
 {
@@ -1084,6 +1101,40 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
   // the usual operator pair (stiffness-only, then mass-only, both folded) in a warp
   // without constrained entries: a loop without per-entry operator branches
   bool const fast = kmPair && !__any_sync(__activemask(), anyBc);
+  if constexpr (T == P2TET)
+  {
+    if (fast)
+    {
+      // the 55 entries unrolled, each with only the reference-tensor terms that can
+      // be nonzero (177 of 330)
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = i; j < N; ++j)
+        {
+          double kv = 0.;
+          bool first = true;
+#pragma unroll
+          for (int k = 0; k < 6; ++k)
+            if (p2Term(k, i, j))
+            {
+              kv = first ? G[k] * TT<T>(k, i, j) : fma(G[k], TT<T>(k, i, j), kv);
+              first = false;
+            }
+          double const mv = am * MHAT<T>(i, j);
+          int32_t const pij = rpn[i] + rk[i * N + j];
+          red(op0.vals + pij, kv);
+          red(op1.vals + pij, mv);
+          if (j != i)
+          {
+            int32_t const pji = rpn[j] + rk[j * N + i];
+            red(op0.vals + pji, kv);
+            red(op1.vals + pji, mv);
+          }
+        }
+      goto entriesDone;
+    }
+  }
 #pragma unroll kRowUnroll
   for (int i = 0; i < N; ++i)
   {
@@ -1148,6 +1199,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
       }
     }
   }
+entriesDone:
   if (!a.b)
     return;
   if (anyBc)

@@ -233,7 +233,10 @@ __device__ __forceinline__ void loadRankRow(uint16_t const * rk, int i, uint16_t
 }
 } // namespace q1f
 
-__global__ void __launch_bounds__(128, 1) kAssembleQ1F64(AsmArgs a)
+// NT threads per block, at least MINB blocks per SM (the register budget per thread:
+// 128 x 1 -> 254 registers, 8 warps per SM; 64 x 6 -> 170 registers, 12 warps per SM)
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
 {
   using namespace q1f;
   int64_t const i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -789,9 +792,10 @@ __global__ void __launch_bounds__(128, 1) kAssembleQ1F64(AsmArgs a)
 
 void launchAssembleQ1F64(AsmArgs const & a, cudaStream_t s, int threads)
 {
-  int const nt = threads == 64 ? 64 : 128;
-  unsigned const blocks = (unsigned)((a.nelem + nt - 1) / nt);
-  kAssembleQ1F64<<<blocks, nt, 0, s>>>(a);
+  if (threads == 64)
+    kAssembleQ1F64<64, 6><<<(unsigned)((a.nelem + 63) / 64), 64, 0, s>>>(a);
+  else
+    kAssembleQ1F64<128, 1><<<(unsigned)((a.nelem + 127) / 128), 128, 0, s>>>(a);
 }
 
 } // namespace pxg

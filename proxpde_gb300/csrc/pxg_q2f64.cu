@@ -118,6 +118,7 @@ struct Smem
   double coef[72];
   double w[NQ];
   double X[8][3];
+  double H[8][3]; // Walsh-Hadamard transform of the vertices, [kx + 2 ky + 4 kz][r]
   double G[6][NQ];
   double ad[NQ];
   double Mt[216];
@@ -175,9 +176,28 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
   double const ks1 = k1 ? (op1.stiff == 2 ? op1.sc * kfac : op1.sc) : 0.;
   double const ms0 = m0 ? massCoef(op0, kfac) : 0., ms1 = m1 ? massCoef(op1, kfac) : 0.;
 
-  // ---- per point: lane q = qx * 9 + qy * 3 + qz.  Walsh-Hadamard transform of the
-  // vertices (every lane, same values): x(xi) = 1/8 sum_k H_k xi^kx eta^ky zeta^kz;
-  // the Jacobian columns (x8) c1 = H100 + eta H110 + zeta H101 + eta zeta H111, ...
+  // ---- the Walsh-Hadamard transform of the vertices, x(xi) = 1/8 sum_k H_k xi^kx
+  // eta^ky zeta^kz: lane 3 lat + r holds coordinate r of the vertex at lattice point
+  // lat = vx + 2 vy + 4 vz (proxpde's Q1 vertex order, src/reffe.cpp:684-759), and
+  // each stage pairs the lanes whose lattice points differ along one axis
+  {
+    int const lat = lane / 3, r = lane % 3;
+    int const vx = lat & 1, vy = (lat >> 1) & 1, vz = lat >> 2;
+    int const v = vz * 4 + (vy ? (vx ? 2 : 3) : (vx ? 1 : 0));
+    double h = lane < 24 ? S.X[v][r] : 0.;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+    {
+      int const bit = (lat >> ax) & 1, step = 3 << ax;
+      double const o = __shfl_sync(0xffffffffu, h, lane < 24 ? (bit ? lane - step : lane + step) : lane);
+      h = bit ? h - o : h + o;
+    }
+    if (lane < 24)
+      S.H[lat][r] = h;
+  }
+  __syncwarp();
+  // ---- per point: lane q = qx * 9 + qy * 3 + qz; the Jacobian columns (x8)
+  // c1 = H100 + eta H110 + zeta H101 + eta zeta H111, ...
   if (lane < NQ)
   {
     int const qx = lane / 9, qy = (lane / 3) % 3, qz = lane % 3;
@@ -187,42 +207,13 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
 #pragma unroll
     for (int r = 0; r < 3; ++r)
     {
-      // vertex v at lattice (vx, vy, vz): proxpde's Q1 vertex order (src/reffe.cpp:684-759)
-      double H[2][2][2];
-#pragma unroll
-      for (int v = 0; v < 8; ++v)
-      {
-        int const vx = (v == 1 || v == 2 || v == 5 || v == 6), vy = (v == 2 || v == 3 || v == 6 || v == 7), vz = v >= 4;
-        H[vx][vy][vz] = S.X[v][r];
-      }
-#pragma unroll
-      for (int y = 0; y < 2; ++y)
-#pragma unroll
-        for (int z = 0; z < 2; ++z)
-        {
-          double const p0 = H[0][y][z], p1 = H[1][y][z];
-          H[0][y][z] = p0 + p1, H[1][y][z] = p1 - p0;
-        }
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
-#pragma unroll
-        for (int z = 0; z < 2; ++z)
-        {
-          double const p0 = H[x][0][z], p1 = H[x][1][z];
-          H[x][0][z] = p0 + p1, H[x][1][z] = p1 - p0;
-        }
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
-#pragma unroll
-        for (int y = 0; y < 2; ++y)
-        {
-          double const p0 = H[x][y][0], p1 = H[x][y][1];
-          H[x][y][0] = p0 + p1, H[x][y][1] = p1 - p0;
-        }
-      c[0][r] = fma(zeta, fma(eta, H[1][1][1], H[1][0][1]), fma(eta, H[1][1][0], H[1][0][0]));
-      c[1][r] = fma(zeta, fma(xi, H[1][1][1], H[0][1][1]), fma(xi, H[1][1][0], H[0][1][0]));
-      c[2][r] = fma(eta, fma(xi, H[1][1][1], H[0][1][1]), fma(xi, H[1][0][1], H[0][0][1]));
-      o[r] = 0.125 * H[0][0][0];
+      // H[kx + 2 ky + 4 kz]
+      double const H000 = S.H[0][r], H100 = S.H[1][r], H010 = S.H[2][r], H110 = S.H[3][r];
+      double const H001 = S.H[4][r], H101 = S.H[5][r], H011 = S.H[6][r], H111 = S.H[7][r];
+      c[0][r] = fma(zeta, fma(eta, H111, H101), fma(eta, H110, H100));
+      c[1][r] = fma(zeta, fma(xi, H111, H011), fma(xi, H110, H010));
+      c[2][r] = fma(eta, fma(xi, H111, H011), fma(xi, H101, H001));
+      o[r] = 0.125 * H000;
     }
     double const g11 = fma(c[0][0], c[0][0], fma(c[0][1], c[0][1], c[0][2] * c[0][2]));
     double const g22 = fma(c[1][0], c[1][0], fma(c[1][1], c[1][1], c[1][2] * c[1][2]));
