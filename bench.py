@@ -242,7 +242,7 @@ def measure_configs(peak_gbs, reps=5):
               "kAssembleTet64<P1>"),
              ("p2tet_64", L.P2TET, meshgen.cube_tet6, 64, 0.15, 0.5, 2, None, "kAssembleTet64<P2>"),
              ("q2hex_48", L.Q2HEX, meshgen.cube_hex, 48, 0.2, 1.0, 2, {"kind": 1, "fn": L.FN_SIN3, "coef": 1.0},
-              "kAssemble<Q2HEX>"))
+              "kAssembleQ2F64"))
     for name, t, gen, n, alpha, sigma, nmat, rhs, kern in cases:
         xyz, conn = gen(n)
         if alpha:
