@@ -37,7 +37,7 @@ ASSEMBLY = {
     "q1hex": (L.Q1HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssembleQ1F64", "kAssembleQ1Group"),
     "p2tet": (L.P2TET, meshgen.cube_tet6, 0.15, 0.5, True, L.FN_CONST, "kAssembleTet64", "kAssembleTet"),
     "p1tet": (L.P1TET, meshgen.cube_tet6, 0.0, None, False, L.FN_CONST, "kAssembleTet64", "kAssembleTet"),
-    "q2hex": (L.Q2HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssemble", "kAssembleQ2"),
+    "q2hex": (L.Q2HEX, meshgen.cube_hex, 0.2, 1.0, True, L.FN_SIN3, "kAssembleQ2F64", "kAssembleQ2"),
 }
 
 
