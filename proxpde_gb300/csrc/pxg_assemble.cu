@@ -20,6 +20,7 @@
 #include <cub/cub.cuh>
 
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "pxg_dfl.h"
@@ -984,28 +985,99 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
 }
 
 // ------------------------------------------------- tetrahedra in FP64 arithmetic
-// kAssembleTet64 (the default for P1/P2): the reference-tensor form of kAssembleTet in
-// IEEE binary64 throughout.  Per element: J from the vertex differences, adj(J),
-// |det J|, G = adj adj^T / |det J| (with a single stiffness operator's coefficient
-// folded in); an entry is the six-term product of G with the reference tensor (FP64
-// constant memory), the mass entry |det J| Mhat_ij (a single mass operator's
-// coefficient folded into |det J|).  About 450 FP64 operations per P2 element
-// against about 1,000 for the per-quadrature-point form of kAssemble.
-// P2 tetrahedron (src/reffe.cpp:542-642, vertices then the edges 01 12 20 03 13 23):
-// bit a of the mask is set where d/dx_a phi_i is not identically zero (phi_1 depends
-// on x only, phi_5 = 4xy on x and y, ...).  A reference-tensor term whose derivative is
-// identically zero is an exact zero in the table, so skipping it changes no value.
-__host__ __device__ constexpr unsigned p2GradMask(int i)
+// kAssembleTet64 (the default for P1/P2) in IEEE binary64 throughout.  Per element:
+// J from the vertex differences, adj(J), |det J|, G = adj adj^T / |det J| (with a
+// single stiffness operator's coefficient folded in).  P1 reads its entries from G
+// directly; P2 with the usual stiffness + mass pair uses the barycentric form below,
+// and otherwise the six-term products of G with the reference tensor (FP64 constant
+// memory).  A mass entry is |det J| Mhat_ij (a single mass operator's coefficient
+// folded into |det J|).  P2 tetrahedron: src/reffe.cpp:542-642, vertices then the
+// edges 01 12 20 03 13 23.
+
+// P2 in barycentric form.  With lambda_0 = 1 - x - y - z, lambda_1..3 = x, y, z, the
+// vertex and edge functions are phi_i = lambda_i (2 lambda_i - 1) and
+// phi_(ab) = 4 lambda_a lambda_b, whose gradients are linear in the lambdas, so with
+// s_kl = k |T| grad lambda_k . grad lambda_l and the exact moments
+// (1/|T|) int lambda_k lambda_l = (1 + delta_kl) / 20 the stiffness entries are short
+// integer combinations of s' = s / 5:
+//   vertex-vertex        K_ii = 3 s'_ii,  K_ij = -s'_ij
+//   vertex i, edge (ab)  i = a: 3 s'_ib - s'_ii;  i not in (ab): -(s'_ia + s'_ib)
+//   edge-edge            the same edge: 8 (s'_aa + s'_bb + s'_ab); sharing vertex v with
+//                        other ends p, q: 4 (s'_vv + s'_vq + s'_pv + 2 s'_pq); disjoint
+//                        (ab), (cd): 4 (s'_ac + s'_ad + s'_bc + s'_bd)
+// The reference's 11-point rule integrates these degree-2 integrands exactly, so the
+// values agree with its per-quadrature-point sums to round-off (114 FP64 operations per
+// element instead of 177 for the reference-tensor products without their zero terms).
+__host__ __device__ constexpr int p2EdgeEnd(int n, int k)
 {
-  return i == 1 ? 1u : i == 2 ? 2u : i == 3 ? 4u : i == 5 ? 3u : i == 8 ? 5u : i == 9 ? 6u : 7u;
+  return k == 0 ? (n == 4 ? 0 : n == 5 ? 1 : n == 6 ? 2 : n == 7 ? 0 : n == 8 ? 1 : 2)
+                : (n == 4 ? 1 : n == 5 ? 2 : n == 6 ? 0 : 3);
 }
-// term k (xx yy zz xy xz yz) of entry (i, j) of the P2 reference tensor can be nonzero
-__host__ __device__ constexpr bool p2Term(int k, int i, int j)
+// exact negation: the sign bit flipped on the integer pipe
+__device__ __forceinline__ double negx(double x)
 {
-  int const a = k < 3 ? k : (k == 5 ? 1 : 0), b = k < 3 ? k : (k == 3 ? 1 : 2);
-  bool const ab = ((p2GradMask(i) >> a) & 1u) && ((p2GradMask(j) >> b) & 1u);
-  bool const ba = ((p2GradMask(i) >> b) & 1u) && ((p2GradMask(j) >> a) & 1u);
-  return k < 3 ? ab : (ab || ba);
+  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+template <int I, int J>
+__device__ __forceinline__ double p2Stiff(double const (&s)[4][4])
+{
+  if constexpr (J < 4)
+    return I == J ? 3.0 * s[I][I] : negx(s[I][J]);
+  else
+  {
+    constexpr int c = p2EdgeEnd(J, 0), d = p2EdgeEnd(J, 1);
+    if constexpr (I < 4)
+    {
+      if constexpr (I == c)
+        return fma(3.0, s[I][d], -s[I][I]);
+      else if constexpr (I == d)
+        return fma(3.0, s[I][c], -s[I][I]);
+      else
+        return -s[I][c] - s[I][d];
+    }
+    else
+    {
+      constexpr int a = p2EdgeEnd(I, 0), b = p2EdgeEnd(I, 1);
+      if constexpr (I == J)
+        return 8.0 * ((s[a][a] + s[b][b]) + s[a][b]);
+      else if constexpr (a == c || a == d || b == c || b == d)
+      {
+        constexpr int v = (a == c || a == d) ? a : b, p = v == a ? b : a, q = c == v ? d : c;
+        return 4.0 * fma(2.0, s[p][q], (s[v][v] + s[v][q]) + s[p][v]);
+      }
+      else
+        return 4.0 * ((s[a][c] + s[a][d]) + (s[b][c] + s[b][d]));
+    }
+  }
+}
+// the seven classes of the P2 mass matrix: vertex-vertex (same, other), vertex-edge
+// (on, off), edge-edge (same, sharing a vertex, disjoint); a representative entry each
+__host__ __device__ constexpr bool p2EdgesMeet(int i, int j)
+{
+  return p2EdgeEnd(i, 0) == p2EdgeEnd(j, 0) || p2EdgeEnd(i, 0) == p2EdgeEnd(j, 1) ||
+         p2EdgeEnd(i, 1) == p2EdgeEnd(j, 0) || p2EdgeEnd(i, 1) == p2EdgeEnd(j, 1);
+}
+__host__ __device__ constexpr int p2MassClass(int i, int j)
+{
+  return j < 4   ? (i == j ? 0 : 1)
+         : i < 4 ? ((i == p2EdgeEnd(j, 0) || i == p2EdgeEnd(j, 1)) ? 2 : 3)
+         : i == j ? 4
+                  : (p2EdgesMeet(i, j) ? 5 : 6);
+}
+__host__ __device__ constexpr int p2MassRepI(int c) { return c < 4 ? 0 : 4; }
+__host__ __device__ constexpr int p2MassRepJ(int c)
+{
+  return c == 0 ? 0 : c == 1 ? 1 : c == 2 ? 4 : c == 3 ? 5 : c == 4 ? 4 : c == 5 ? 5 : 9;
+}
+// f(I, J) for the 55 pairs I <= J of the P2 element, as compile-time constants
+template <int I, int J, class F>
+__device__ __forceinline__ void p2ForPairs(F && f)
+{
+  f(std::integral_constant<int, I>{}, std::integral_constant<int, J>{});
+  if constexpr (J + 1 < 10)
+    p2ForPairs<I, J + 1>(f);
+  else if constexpr (I + 1 < 10)
+    p2ForPairs<I + 1, I + 1>(f);
 }
 
 template <int T, int NT>
@@ -1066,8 +1138,20 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
     double const e = fma(-adet, ra, 1.0);
     ra = fma(ra, fma(e, e, e), ra);
   }
+  bool const anyBc = cons && ((op0.on && op0.bc) || (op1.on && op1.bc));
+  bool const kmPair = op0.on && op0.stiff && !op0.mass && op1.on && !op1.stiff && op1.mass;
+  // the usual operator pair (stiffness-only, then mass-only, both folded) in a warp
+  // without constrained entries: a loop without per-entry operator branches
+  bool const fast = kmPair && !__any_sync(__activemask(), anyBc);
   double G[6];
-  gram(A, (foldK ? (k0 ? ks0 : ks1) : 1.0) * (T == P1TET ? ra * cP1Ws : ra), G);
+  {
+    double gs = (foldK ? (k0 ? ks0 : ks1) : 1.0) * ra;
+    if constexpr (T == P1TET)
+      gs *= cP1Ws;
+    else if (fast)
+      gs *= 1.0 / 30.0; // s'_(a+1)(b+1) = G_ab of the barycentric form
+    gram(A, gs, G);
+  }
   double const am = foldM ? (m0 ? ms0 : ms1) * adet : adet;
   // P1: grad phi_i |det J| are the adjugate rows (i = 1..3) and minus their sum (i = 0),
   // so K_ij = k / (6 |det J|) A_i . A_j reads the Gram entries of the adjugate directly:
@@ -1094,44 +1178,45 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
 #pragma unroll
   for (int n = 0; n < N; ++n)
     rpn[n] = a.rowPtr[dof[n]];
-  bool const anyBc = cons && ((op0.on && op0.bc) || (op1.on && op1.bc));
   uint16_t const * rk = a.rank + e * (int64_t)(N * N);
   constexpr int kRowUnroll = N <= 4 ? N : 1;
-  bool const kmPair = op0.on && op0.stiff && !op0.mass && op1.on && !op1.stiff && op1.mass;
-  // the usual operator pair (stiffness-only, then mass-only, both folded) in a warp
-  // without constrained entries: a loop without per-entry operator branches
-  bool const fast = kmPair && !__any_sync(__activemask(), anyBc);
   if constexpr (T == P2TET)
   {
     if (fast)
     {
-      // the 55 entries unrolled, each with only the reference-tensor terms that can
-      // be nonzero (177 of 330)
+      // the 55 entries unrolled in the barycentric form (the adjugate rows are the
+      // gradients of lambda_1..3 times det J, lambda_0's is minus their sum) and the
+      // mass from its seven distinct values
+      double s[4][4];
+      s[1][1] = G[0];
+      s[2][2] = G[1];
+      s[3][3] = G[2];
+      s[1][2] = s[2][1] = G[3];
+      s[1][3] = s[3][1] = G[4];
+      s[2][3] = s[3][2] = G[5];
+      double const c1 = G[0] + (G[3] + G[4]), c2 = G[3] + (G[1] + G[5]), c3 = G[4] + (G[5] + G[2]);
+      s[0][1] = s[1][0] = negx(c1);
+      s[0][2] = s[2][0] = negx(c2);
+      s[0][3] = s[3][0] = negx(c3);
+      s[0][0] = c1 + (c2 + c3);
+      double mc[7];
 #pragma unroll
-      for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = i; j < N; ++j)
+      for (int c = 0; c < 7; ++c)
+        mc[c] = am * MHAT<T>(p2MassRepI(c), p2MassRepJ(c));
+      p2ForPairs<0, 0>([&](auto I, auto J) {
+        constexpr int i = decltype(I)::value, j = decltype(J)::value;
+        double const kv = p2Stiff<i, j>(s);
+        double const mv = mc[p2MassClass(i, j)];
+        int32_t const pij = rpn[i] + rk[i * N + j];
+        red(op0.vals + pij, kv);
+        red(op1.vals + pij, mv);
+        if constexpr (j != i)
         {
-          double kv = 0.;
-          bool first = true;
-#pragma unroll
-          for (int k = 0; k < 6; ++k)
-            if (p2Term(k, i, j))
-            {
-              kv = first ? G[k] * TT<T>(k, i, j) : fma(G[k], TT<T>(k, i, j), kv);
-              first = false;
-            }
-          double const mv = am * MHAT<T>(i, j);
-          int32_t const pij = rpn[i] + rk[i * N + j];
-          red(op0.vals + pij, kv);
-          red(op1.vals + pij, mv);
-          if (j != i)
-          {
-            int32_t const pji = rpn[j] + rk[j * N + i];
-            red(op0.vals + pji, kv);
-            red(op1.vals + pji, mv);
-          }
+          int32_t const pji = rpn[j] + rk[j * N + i];
+          red(op0.vals + pji, kv);
+          red(op1.vals + pji, mv);
         }
+      });
       goto entriesDone;
     }
   }
