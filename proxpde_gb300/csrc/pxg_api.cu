@@ -128,6 +128,7 @@ pxg_status pxg_create(pxg_ctx ** out, int device)
   c->q1Group = envOn("PXG_Q1_GROUP");
   c->tetGeneric = envOn("PXG_TET_GENERIC");
   c->q2Generic = envOn("PXG_Q2_GENERIC");
+  c->groupScatter = !envOn("PXG_NO_GROUP_SCATTER");
   pxg_status s = ensureDevice(c);
   if (s == PXG_OK && cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
     s = cudaFail(c, cudaGetLastError(), "SM count");
@@ -193,6 +194,7 @@ pxg_status pxg_set_mesh(pxg_ctx * c, int etype, double const * xyz, int64_t nnod
   c->rowPtr.reset();
   c->colIdx.reset();
   c->rank.reset();
+  c->groups.reset();
   c->kE.reset();
   c->hasCoef = false;
   c->colour.perm.reset();
@@ -273,6 +275,7 @@ pxg_status pxg_build_dofmap(pxg_ctx * c, int64_t * ndof)
   c->rowPtr.reset();
   c->colIdx.reset();
   c->rank.reset();
+  c->groups.reset();
   c->nnz = 0;
   if ((s = buildDofmap(c)) != PXG_OK)
     return s;
@@ -317,6 +320,7 @@ pxg_status pxg_set_dofmap(pxg_ctx * c, uint32_t const * em, int64_t ndof, int me
   c->rowPtr.reset();
   c->colIdx.reset();
   c->rank.reset();
+  c->groups.reset();
   c->nnz = 0;
   c->bcMask.reset();
   c->bcVal.reset();

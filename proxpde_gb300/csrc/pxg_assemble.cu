@@ -1008,11 +1008,6 @@ __global__ void __launch_bounds__(NT) kAssembleTet(AsmArgs a)
 // The reference's 11-point rule integrates these degree-2 integrands exactly, so the
 // values agree with its per-quadrature-point sums to round-off (114 FP64 operations per
 // element instead of 177 for the reference-tensor products without their zero terms).
-__host__ __device__ constexpr int p2EdgeEnd(int n, int k)
-{
-  return k == 0 ? (n == 4 ? 0 : n == 5 ? 1 : n == 6 ? 2 : n == 7 ? 0 : n == 8 ? 1 : 2)
-                : (n == 4 ? 1 : n == 5 ? 2 : n == 6 ? 0 : 3);
-}
 // exact negation: the sign bit flipped on the integer pipe
 __device__ __forceinline__ double negx(double x)
 {
@@ -1050,20 +1045,7 @@ __device__ __forceinline__ double p2Stiff(double const (&s)[4][4])
     }
   }
 }
-// the seven classes of the P2 mass matrix: vertex-vertex (same, other), vertex-edge
-// (on, off), edge-edge (same, sharing a vertex, disjoint); a representative entry each
-__host__ __device__ constexpr bool p2EdgesMeet(int i, int j)
-{
-  return p2EdgeEnd(i, 0) == p2EdgeEnd(j, 0) || p2EdgeEnd(i, 0) == p2EdgeEnd(j, 1) ||
-         p2EdgeEnd(i, 1) == p2EdgeEnd(j, 0) || p2EdgeEnd(i, 1) == p2EdgeEnd(j, 1);
-}
-__host__ __device__ constexpr int p2MassClass(int i, int j)
-{
-  return j < 4   ? (i == j ? 0 : 1)
-         : i < 4 ? ((i == p2EdgeEnd(j, 0) || i == p2EdgeEnd(j, 1)) ? 2 : 3)
-         : i == j ? 4
-                  : (p2EdgesMeet(i, j) ? 5 : 6);
-}
+// a representative entry of each P2 mass class
 __host__ __device__ constexpr int p2MassRepI(int c) { return c < 4 ? 0 : 4; }
 __host__ __device__ constexpr int p2MassRepJ(int c)
 {
@@ -1174,10 +1156,12 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
     K1[0][0] = cs[0] + (cs[1] + cs[2]);
   }
 
+  // the warp-group scatter of P2 finds its positions in its own map
+  bool const grouped = T == P2TET && fast && a.grpOff;
   int32_t rpn[N];
 #pragma unroll
   for (int n = 0; n < N; ++n)
-    rpn[n] = a.rowPtr[dof[n]];
+    rpn[n] = grouped ? 0 : a.rowPtr[dof[n]];
   uint16_t const * rk = a.rank + e * (int64_t)(N * N);
   constexpr int kRowUnroll = N <= 4 ? N : 1;
   if constexpr (T == P2TET)
@@ -1203,6 +1187,69 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
 #pragma unroll
       for (int c = 0; c < 7; ++c)
         mc[c] = am * MHAT<T>(p2MassRepI(c), p2MassRepJ(c));
+      if (a.grpOff)
+      {
+        // warp-group scatter: the lane's values and the group's contribution codes to
+        // shared memory, then one reduction per distinct position of the warp's 32
+        // elements, in ascending order
+        extern __shared__ double gsm[];
+        int const lane = threadIdx.x & 31;
+        unsigned char * const wbase = reinterpret_cast<unsigned char *>(gsm) + (threadIdx.x >> 5) * kP2GroupSmemPerWarp;
+        double * const sw = reinterpret_cast<double *>(wbase);
+        uint16_t * const si = reinterpret_cast<uint16_t *>(wbase + kP2GroupValues * 32 * sizeof(double));
+        p2ForPairs<0, 0>([&](auto I, auto J) {
+          constexpr int i = decltype(I)::value, j = decltype(J)::value;
+          sw[p2UpperIdx(i, j) * 32 + lane] = p2Stiff<i, j>(s);
+        });
+#pragma unroll
+        for (int c = 0; c < 7; ++c)
+          sw[(55 + c) * 32 + lane] = mc[c];
+        unsigned const mask = __activemask();
+        int const W = __popc(mask); // the active lanes are 0 .. W - 1
+        int64_t const g = e >> 5;
+        // the group's codes: W * 100 of them, 16 bytes (8 codes) per load; the map pads
+        // the last group's codes to a multiple of 8
+        int const nItems = W * 100;
+        uint4 const * const gi = reinterpret_cast<uint4 const *>(a.grpItem + g * kP2GroupItems);
+        for (int k = lane; k < (nItems + 7) / 8; k += W)
+          reinterpret_cast<uint4 *>(si)[k] = gi[k];
+        __syncwarp(mask);
+        int32_t const dEnd = a.grpOff[g + 1];
+        constexpr int U = 4;
+        for (int32_t d0 = a.grpOff[g]; d0 < dEnd; d0 += U * W)
+        {
+          int32_t pos[U];
+          int b0[U], b1[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+          {
+            int32_t const d = d0 + u * W + lane;
+            pos[u] = d < dEnd ? a.grpPos[d] : 0;
+            b0[u] = d < dEnd ? a.grpBeg[d] : 0;
+            b1[u] = d + 1 < dEnd ? a.grpBeg[d + 1] : nItems;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+          {
+            if (d0 + u * W + lane >= dEnd)
+              break;
+            // the position's contributions in element order: no addition for the
+            // first (the FP64 pipe is the scarce one)
+            uint32_t code = si[b0[u]];
+            double kk = sw[((code >> 5) & 63u) * 32 + (code & 31u)];
+            double mm = sw[(55 + (code >> 11)) * 32 + (code & 31u)];
+            for (int k = b0[u] + 1; k < b1[u]; ++k)
+            {
+              code = si[k];
+              kk += sw[((code >> 5) & 63u) * 32 + (code & 31u)];
+              mm += sw[(55 + (code >> 11)) * 32 + (code & 31u)];
+            }
+            red(op0.vals + pos[u], kk);
+            red(op1.vals + pos[u], mm);
+          }
+        }
+        goto entriesDone;
+      }
       p2ForPairs<0, 0>([&](auto I, auto J) {
         constexpr int i = decltype(I)::value, j = decltype(J)::value;
         double const kv = p2Stiff<i, j>(s);
@@ -1904,7 +1951,14 @@ void launchAssembleTet64(AsmArgs const & a, cudaStream_t s, int threads)
 {
   auto go = [&](auto kern, int nt) {
     unsigned const blocks = (unsigned)((a.nelem + nt - 1) / nt);
-    kern<<<blocks, nt, 0, s>>>(a);
+    size_t smem = 0;
+    if (T == P2TET && a.grpOff)
+    {
+      // the warp-group scatter's values and codes
+      smem = (size_t)(nt / 32) * kP2GroupSmemPerWarp;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    kern<<<blocks, nt, smem, s>>>(a);
   };
   if (threads == 64)
     return go(kAssembleTet64<T, 64>, 64);
@@ -2152,7 +2206,19 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
       if (c->tetGeneric)
         launchAssemble<P2TET>(la, s, c->threads);
       else if (fp64)
-        launchAssembleTet64<P2TET>(la, s, c->threads);
+      {
+        AsmArgs lg = la;
+        if (!la.perm && c->groups.built && c->groupScatter)
+        {
+          lg.grpOff = c->groups.off.p;
+          lg.grpPos = c->groups.pos.p;
+          lg.grpBeg = c->groups.beg.p;
+          lg.grpItem = c->groups.item.p;
+        }
+        // the warp-group scatter's shared memory favours small blocks (64 threads: ten
+        // warps per SM), so that is its default
+        launchAssembleTet64<P2TET>(lg, s, c->threads ? c->threads : (lg.grpOff ? 64 : 128));
+      }
       else
         launchAssembleTet<P2TET>(la, s, c->threads);
       break;
@@ -2185,6 +2251,16 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
     }
     launchValuesLoad(la);
   };
+  // the warp-group scatter map of the P2 FP64 kernel, on first use outside a capture
+  // (inside one, the kernel adds its entries one by one)
+  if (c->etype == P2TET && c->arith == PXG_ARITH_FP64 && c->scatter == PXG_SCATTER_REDUCE && c->groupScatter &&
+      !c->tetGeneric && !c->groups.built && (a.op[0].on || a.op[1].on))
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PXG_CUDA(c, cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone && (st = buildScatterGroups(c)) != PXG_OK)
+      return st;
+  }
   if (c->scatter == PXG_SCATTER_COLOUR)
   {
     if (!c->colour.built)

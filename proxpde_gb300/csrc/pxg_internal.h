@@ -310,6 +310,27 @@ struct pxg_ctx
     pxg::DevBuf<uint32_t> perm;
     bool built = false;
   } colour;
+  // warp-group scatter map of the P2 FP64 kernel (pxg_group.cu): for each group of 32
+  // consecutive elements, its distinct CSR positions in ascending order (off: first
+  // index of each group, pos, beg: offset of the first contribution in the group) and
+  // the contributions in the same order as codes (element lane | local entry); built
+  // on first use
+  struct GroupState
+  {
+    bool built = false;
+    int64_t ngroups = 0, ndistinct = 0;
+    pxg::DevBuf<int32_t> off, pos;
+    pxg::DevBuf<uint16_t> beg, item;
+    void reset()
+    {
+      built = false;
+      ngroups = ndistinct = 0;
+      off.reset();
+      pos.reset();
+      beg.reset();
+      item.reset();
+    }
+  } groups;
   // boundary facets in key order: element * faces-per-element + local face, and markers
   struct FacetState
   {
@@ -331,6 +352,8 @@ struct pxg_ctx
   bool q1Group = false;
   bool tetGeneric = false;
   bool q2Generic = false;
+  // P2 FP64: sum each warp's contributions per distinct position before the reductions
+  bool groupScatter = true;
   int sms = 0; // SMs of the device (persistent grids)
   // What produced each value array pxg_assemble wrote (its recipe): the lhs operators
   // added into it since it was last overwritten, with the versions of the coordinates,
@@ -402,7 +425,51 @@ struct AsmArgs
   // colour-ordered scatter: the launch covers elements perm[permBase .. permBase + nelem)
   uint32_t const * perm;
   int64_t permBase;
+  // warp-group scatter map (P2 FP64 kernel, element order only; null: plain reductions)
+  int32_t const * grpOff;
+  int32_t const * grpPos;
+  uint16_t const * grpBeg;
+  uint16_t const * grpItem;
 };
+
+// P2 tetrahedron local numbering (src/reffe.cpp:542-642): vertices 0-3, then the edges
+// 01 12 20 03 13 23 as nodes 4-9; end k of edge node n
+__host__ __device__ constexpr int p2EdgeEnd(int n, int k)
+{
+  return k == 0 ? (n == 4 ? 0 : n == 5 ? 1 : n == 6 ? 2 : n == 7 ? 0 : n == 8 ? 1 : 2)
+                : (n == 4 ? 1 : n == 5 ? 2 : n == 6 ? 0 : 3);
+}
+__host__ __device__ constexpr bool p2EdgesMeet(int i, int j)
+{
+  return p2EdgeEnd(i, 0) == p2EdgeEnd(j, 0) || p2EdgeEnd(i, 0) == p2EdgeEnd(j, 1) ||
+         p2EdgeEnd(i, 1) == p2EdgeEnd(j, 0) || p2EdgeEnd(i, 1) == p2EdgeEnd(j, 1);
+}
+// the seven classes of the P2 mass matrix: vertex-vertex (same, other), vertex-edge
+// (on, off), edge-edge (same, sharing a vertex, disjoint)
+__host__ __device__ constexpr int p2MassClass(int i, int j)
+{
+  return j < i   ? p2MassClass(j, i)
+         : j < 4 ? (i == j ? 0 : 1)
+         : i < 4 ? ((i == p2EdgeEnd(j, 0) || i == p2EdgeEnd(j, 1)) ? 2 : 3)
+         : i == j ? 4
+                  : (p2EdgesMeet(i, j) ? 5 : 6);
+}
+// index of the pair (min, max) among the 55 pairs i <= j of the P2 element, row by row
+__host__ __device__ constexpr int p2UpperIdx(int i, int j)
+{
+  return j < i ? p2UpperIdx(j, i) : i * 10 - i * (i - 1) / 2 + (j - i);
+}
+// warp-group scatter of the P2 kernel: per warp, the 55 stiffness entries and the 7 mass
+// values of each lane's element in shared memory, value-major (value v of lane l at
+// v * 32 + l), then the group's 3,200 contribution codes; a code is
+// lane | pair index << 5 | mass class << 11
+constexpr int kP2GroupValues = 55 + 7;
+constexpr int kP2GroupItems = 32 * 100;
+constexpr size_t kP2GroupSmemPerWarp = kP2GroupValues * 32 * sizeof(double) + kP2GroupItems * sizeof(uint16_t);
+__host__ __device__ constexpr uint16_t p2GroupCode(int lane, int i, int j)
+{
+  return (uint16_t)(lane | (p2UpperIdx(i, j) << 5) | (p2MassClass(i, j) << 11));
+}
 
 // element id of the launch's i-th element
 __device__ __forceinline__ int64_t elemOf(AsmArgs const & a, int64_t i)
@@ -502,6 +569,7 @@ pxg_status initQ2Tables(pxg_ctx * c);                      // pxg_q2.cu
 void launchAssembleQ2(AsmArgs const & a, cudaStream_t s, int sms); // pxg_q2.cu
 pxg_status initQ2F64Tables(pxg_ctx * c);                          // pxg_q2f64.cu
 void launchAssembleQ2F64(AsmArgs const & a, cudaStream_t s);      // pxg_q2f64.cu
+pxg_status buildScatterGroups(pxg_ctx * c);                       // pxg_group.cu
 void hostShape(int t, double const * p, double * phi, double * dphi);
 // g_e = -(C u)_e^T K_e (C lambda)_e for every element (pxg_assemble.cu)
 pxg_status launchAdjointGrad(pxg_ctx * c, double const * u, double const * lam, double * g, cudaStream_t s);

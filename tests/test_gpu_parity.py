@@ -227,18 +227,20 @@ def test_q1_kernels_agree_with_oracle(engine, monkeypatch, kernel, bc, n):
     assert_close(g["b"], b, what=f"q1 {kernel} b", eps=eps)
 
 
-@pytest.mark.parametrize("kernel", ["fp64", "dfl", "generic"])
+@pytest.mark.parametrize("kernel", ["fp64", "fp64-plain", "dfl", "generic"])
 @pytest.mark.parametrize("t,gen,n", [(O.P1TET, "tet6", 9), (O.P2TET, "tet6", 5), (O.P2TET, "tet5", 4)],
                          ids=["p1tet6", "p2tet6", "p2tet5"])
 @pytest.mark.parametrize("bc", [False, True], ids=["nobc", "bc"])
 @pytest.mark.parametrize("rhs_fn", ["const", "sin3"])
 def test_tet_kernels_agree_with_oracle(engine, monkeypatch, kernel, t, gen, n, bc, rhs_fn):
     """The tetrahedron kernels against the oracle: reference-tensor entries in FP64
-    (default) and in double-float, and the per-quadrature-point FP64 kernel
+    (default; P2 with the warp-group scatter, and with plain reductions:
+    PXG_NO_GROUP_SCATTER=1) and in double-float, and the per-quadrature-point FP64 kernel
     (PXG_TET_GENERIC=1); K(k_e) + M with a load (the constant load takes the closed-form
     path of the reference-tensor kernels), with and without inhomogeneous Dirichlet
-    data."""
+    data.  750 P2 elements leave the last warp group partly filled."""
     monkeypatch.setenv("PXG_TET_GENERIC", "1" if kernel == "generic" else "0")
+    monkeypatch.setenv("PXG_NO_GROUP_SCATTER", "1" if kernel == "fp64-plain" else "0")
     arith = ARITH_DFL if kernel == "dfl" else ARITH_FP64
     xyz, conn, k = problem(gen, n, 0.15, seed=23, sigma=0.5)
     em, ndof = O.dofmap(t, xyz.shape[0], conn)

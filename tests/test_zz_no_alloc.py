@@ -11,6 +11,7 @@ This file is named to be collected last, so that a failure here does not hide th
 results of the other tests in a run that stops at the first failure.
 """
 import ctypes as C
+import gc
 
 import numpy as np
 import pytest
@@ -71,9 +72,9 @@ def test_noalloc_ragged_csr_and_no_allocation(engine, nrows):
     """A ragged synthetic CSR (empty rows included; values of both signs, exact zeros,
     1e-17, exactly 1e-16 and just above it) with more rows than one block-total scan
     thread covers, up to the 4,194,304-row maximum, against numpy's prune; and the
-    call allocates no device memory: torch's allocator and the device's free memory
-    (cudaMemGetInfo) are unchanged across it, after a first call that sets up the
-    scratch address."""
+    call allocates no device memory: torch's allocator is unchanged across it and the
+    device's free memory (cudaMemGetInfo) does not drop, after a first call that sets
+    up the scratch address."""
     import torch
 
     from proxpde_gb300 import _lib
@@ -112,14 +113,21 @@ def test_noalloc_ragged_csr_and_no_allocation(engine, nrows):
         return n_out.value
 
     assert call() == m
-    torch.cuda.synchronize()
-    free0, _ = torch.cuda.mem_get_info()
-    alloc0 = torch.cuda.memory_allocated()
-    assert call() == m
-    torch.cuda.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
+    # objects of earlier tests that the garbage collector destroys during the window
+    # would release device memory; an allocation by the call can only lower it
+    gc.collect()
+    gc.disable()
+    try:
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        alloc0 = torch.cuda.memory_allocated()
+        assert call() == m
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+    finally:
+        gc.enable()
     assert torch.cuda.memory_allocated() == alloc0
-    assert free1 == free0, (free0, free1)
+    assert free1 >= free0, (free0, free1)
     assert np.array_equal(out_rp.cpu().numpy(), rp_ref)
     assert np.array_equal(out_ci[:m].cpu().numpy(), ci[keep])
     assert np.array_equal(out_v[:m].cpu().numpy(), vals[keep])
