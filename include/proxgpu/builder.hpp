@@ -661,15 +661,79 @@ struct AssemblyDiv
   static constexpr int kind = PXG_OP_DIV;
 };
 
-// CSR matrix on the host; ctx is the engine context (GPU) that assembled it
+// The closed matrix on the host, with the parts of Eigen::SparseMatrix's interface that
+// proxpde's tests use on builder.A (rows/cols/nonZeros/isCompressed, coeff, A * x,
+// norm, block; test/cavitytime.cpp:192, test/solver_test.cpp:74, test/stokes3dhex.cpp:77).
+// The storage is compressed rows (outer = row pointers, inner = column indices), where
+// Eigen's default is compressed columns: the two coincide for the symmetric matrices of
+// the Poisson and Stokes tests, and coeff, operator* and block follow the row-major
+// meaning in every case.  ctx is the engine context (GPU) that assembled it.
 struct CsrMatrix
 {
-  int64_t rows = 0, cols = 0;
+  int64_t nrows = 0, ncols = 0;
   std::vector<int32_t> outer; // row_ptr
   std::vector<int32_t> inner; // col_idx
   std::vector<double> values;
   pxg_ctx * ctx = nullptr;
+
+  int64_t rows() const { return nrows; }
+  int64_t cols() const { return ncols; }
   int64_t nonZeros() const { return (int64_t)values.size(); }
+  bool isCompressed() const { return true; }
+  int32_t const * outerIndexPtr() const { return outer.data(); }
+  int32_t const * innerIndexPtr() const { return inner.data(); }
+  double const * valuePtr() const { return values.data(); }
+  // entry (i, j), 0 where the pattern has none (columns are sorted within a row)
+  double coeff(int64_t i, int64_t j) const
+  {
+    auto const b0 = inner.begin() + outer[i], b1 = inner.begin() + outer[i + 1];
+    auto const it = std::lower_bound(b0, b1, (int32_t)j);
+    return (it != b1 && *it == j) ? values[it - inner.begin()] : 0.;
+  }
+  Vec operator*(Vec const & x) const
+  {
+    if ((int64_t)x.size() != ncols)
+      throw Error(PXG_ERR_INVALID_ARG, "CsrMatrix * Vec: sizes differ");
+    Vec y((size_t)nrows, 0.);
+    for (int64_t i = 0; i < nrows; ++i)
+    {
+      double s = 0.;
+      for (int32_t k = outer[i]; k < outer[i + 1]; ++k)
+        s += values[k] * x[inner[k]];
+      y[i] = s;
+    }
+    return y;
+  }
+  // the Frobenius norm
+  double norm() const
+  {
+    double s = 0.;
+    for (double v: values)
+      s += v * v;
+    return std::sqrt(s);
+  }
+  // a copy of rows r0 .. r0 + nr, columns c0 .. c0 + nc
+  CsrMatrix block(int64_t r0, int64_t c0, int64_t nr, int64_t nc) const
+  {
+    if (r0 < 0 || c0 < 0 || r0 + nr > nrows || c0 + nc > ncols)
+      throw Error(PXG_ERR_INVALID_ARG, "CsrMatrix::block: out of range");
+    CsrMatrix B;
+    B.nrows = nr;
+    B.ncols = nc;
+    B.ctx = ctx;
+    B.outer.push_back(0);
+    for (int64_t i = r0; i < r0 + nr; ++i)
+    {
+      for (int32_t k = outer[i]; k < outer[i + 1]; ++k)
+        if (inner[k] >= c0 && inner[k] < c0 + nc)
+        {
+          B.inner.push_back((int32_t)(inner[k] - c0));
+          B.values.push_back(values[k]);
+        }
+      B.outer.push_back((int32_t)B.inner.size());
+    }
+    return B;
+  }
 };
 
 // UmfPackLU's interface as the tests use it (include/sparse_matrix.hpp:44:
@@ -688,14 +752,14 @@ struct LUSolver
 
   void analyzePattern(CsrMatrix const & A)
   {
-    if (!A.ctx || A.rows != A.cols || (int64_t)A.outer.size() != A.rows + 1)
+    if (!A.ctx || A.rows() != A.cols() || (int64_t)A.outer.size() != A.rows() + 1)
       throw Error(PXG_ERR_INVALID_ARG, "LUSolver: a square matrix closed by a Builder is needed");
     ctx = A.ctx;
-    n = A.rows;
+    n = A.rows();
   }
   void factorize(CsrMatrix const & A)
   {
-    if (A.ctx != ctx || A.rows != n)
+    if (A.ctx != ctx || A.rows() != n)
       throw Error(PXG_ERR_INVALID_ARG, "LUSolver: factorize a matrix of the analysed pattern");
     rp = DeviceArray<int32_t>(ctx, A.outer.size());
     ci = DeviceArray<int32_t>(ctx, std::max<size_t>(A.inner.size(), 1));
@@ -734,7 +798,7 @@ struct Builder
   DeviceArray<double> vals; // accumulated values on the structural pattern
   DeviceArray<double> bDev;
   CsrMatrix A;
-  std::vector<double> b;
+  Vec b;
 
   explicit Builder(FE & f):
       fe(f), vals(f.ctx, (size_t)f.nnz), bDev(f.ctx, (size_t)f.dof.size), b((size_t)f.dof.size, 0.0)
@@ -771,7 +835,7 @@ struct Builder
     DeviceArray<double> vo(fe.ctx, (size_t)fe.nnz);
     int64_t nnz = 0;
     check(pxg_close_matrix(fe.ctx, vals.p, rp.p, ci.p, vo.p, &nnz, nullptr), fe.ctx, "pxg_close_matrix");
-    A.rows = A.cols = n;
+    A.nrows = A.ncols = n;
     A.ctx = fe.ctx;
     A.outer = rp.host();
     A.inner = ci.host();
@@ -907,7 +971,7 @@ struct Builder<void, Storage>
 {
   int64_t size;
   CsrMatrix A;
-  std::vector<double> b;
+  Vec b;
 
   explicit Builder(int64_t n): size(n), b((size_t)n, 0.0) {}
 
@@ -1048,7 +1112,7 @@ struct Builder<void, Storage>
     DeviceArray<double> vo(c0, (size_t)nnz);
     int64_t kept = 0;
     check(pxg_sys_close_matrix(S, vals.p, rpo.p, cio.p, vo.p, &kept, nullptr), c0, "pxg_sys_close_matrix");
-    A.rows = A.cols = ntot;
+    A.nrows = A.ncols = ntot;
     A.ctx = c0;
     A.outer = rpo.host();
     A.inner = cio.host();

@@ -29,7 +29,7 @@ int run(int n, char const * out)
   FILE * f = std::fopen(out, "wb");
   if (!f)
     return 2;
-  int64_t const hdr[2] = {builder.A.rows, builder.A.nonZeros()};
+  int64_t const hdr[2] = {builder.A.rows(), builder.A.nonZeros()};
   std::fwrite(hdr, sizeof(hdr), 1, f);
   std::fwrite(builder.A.outer.data(), 4, builder.A.outer.size(), f);
   std::fwrite(builder.A.inner.data(), 4, builder.A.inner.size(), f);

@@ -55,7 +55,7 @@ int run(char const * out)
   FILE * f = std::fopen(out, "wb");
   if (!f)
     return 1;
-  int64_t const hdr[3] = {builder.A.rows, builder.A.nonZeros(), dofU};
+  int64_t const hdr[3] = {builder.A.rows(), builder.A.nonZeros(), dofU};
   std::fwrite(hdr, 8, 3, f);
   std::fwrite(builder.A.outer.data(), 4, builder.A.outer.size(), f);
   std::fwrite(builder.A.inner.data(), 4, builder.A.inner.size(), f);
