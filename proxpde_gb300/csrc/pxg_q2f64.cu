@@ -17,8 +17,11 @@
 //  - stiffness tables, each three one-axis contractions of one G component with the
 //    1D products D_ab = l'_a l'_b, P_ab = l_a l_b (6 symmetric classes) or
 //    E_ab = l'_a l_b (9): S_x = sum G_xx D P P, S_y, S_z (216 values each) and
-//    U_xy = sum G_xy E E P, U_xz, U_yz (486 each); an entry K_ij is a sum of nine
-//    table values (three S, two of each U);
+//    U_xy = sum G_xy E E P, U_xz, U_yz (486 each), the 6-class axis contracted first;
+//    the stiffness stages use each class's three coefficients divided by the first, so
+//    that an output costs two FP64 operations, and an entry K_ij, a sum of nine table
+//    values (three S, two of each U), multiplies each by its deferred scale (the
+//    product of the three classes' first coefficients) in the FMA that adds it;
 //  - mass table sum |det J| w P P P (216), M_ij one value of it;
 //  - the load r_q = w_q |det J_q| f(qpoint_q), contracted to the nodes with l_a.
 // About 16k FP64 operations per element against about 100k for the per-point form.
@@ -39,6 +42,8 @@ constexpr int NQ = 27, N = 27, NP = N * (N + 1) / 2;
 // [0, 9) l_a(t_k) at 3a + k; [9, 27) P classes; [27, 45) D classes; [45, 72) E_ab at
 // 3(3a + b) + k.  Symmetric classes: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2).
 __device__ double gCoef[72];
+__device__ double gCoefN[72];      // P, D, E classes divided by their first coefficient
+__device__ double gScale[3 * 216 + 3 * 486]; // deferred scale of every stiffness table value
 __device__ double gT[3];           // t_k
 __device__ double gWl[NQ];         // weights in lattice order qx * 9 + qy * 3 + qz
 __device__ uint8_t gRuleOfLat[NQ]; // the rule's point index of each lattice point
@@ -72,6 +77,25 @@ __device__ __forceinline__ void stage(double const * in, int m, int C, double co
     out[o] = fma(k[2], in[2 * m + r], fma(k[1], in[m + r], k[0] * in[r]));
   }
   __syncwarp();
+}
+// the same with normalised coefficients (coef[3c] = 1): two operations per output
+__device__ __forceinline__ void stageN(double const * in, int m, int C, double const * coef, double * out, int lane)
+{
+  for (int o = lane; o < m * C; o += 32)
+  {
+    int const r = o / C, c = o - r * C;
+    double const * k = coef + 3 * c;
+    out[o] = fma(k[2], in[2 * m + r], fma(k[1], in[m + r], in[r]));
+  }
+  __syncwarp();
+}
+__device__ __forceinline__ void contract3N(double const * in, int c0, double const * k0, int c1, double const * k1,
+                                           int c2, double const * k2, double * out, double * scr0, double * scr1,
+                                           int lane)
+{
+  stageN(in, 9, c0, k0, scr0, lane);
+  stageN(scr0, 3 * c0, c1, k1, scr1, lane);
+  stageN(scr1, c0 * c1, c2, k2, out, lane);
 }
 // three stages of a [3][3][3] array with the coefficient tables of the three axes
 __device__ __forceinline__ void contract3(double const * in, int c0, double const * k0, int c1, double const * k1,
@@ -116,6 +140,7 @@ __device__ __noinline__ double evalPoint(int fn, double rc, double x, double y, 
 struct Smem
 {
   double coef[72];
+  double coefN[72];
   double w[NQ];
   double X[8][3];
   double H[8][3]; // Walsh-Hadamard transform of the vertices, [kx + 2 ky + 4 kz][r]
@@ -139,7 +164,7 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
   __shared__ Smem S;
   int const lane = threadIdx.x;
   for (int k = lane; k < 72; k += 32)
-    S.coef[k] = gCoef[k];
+    S.coef[k] = gCoef[k], S.coefN[k] = gCoefN[k];
   if (lane < NQ)
   {
     S.w[lane] = gWl[lane];
@@ -234,7 +259,8 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
     // k w |det J| (J^T J)^-1 = k w adj rsqrt(D) / 8 (the columns carry x8)
     double const sG = ((foldK ? (k0 ? ks0 : ks1) : 1.0) * 0.125) * (wq * rs);
     S.G[0][lane] = sG * A11, S.G[1][lane] = sG * A22, S.G[2][lane] = sG * A33;
-    S.G[3][lane] = sG * A12, S.G[4][lane] = sG * A13, S.G[5][lane] = sG * A23;
+    // G_xy as [qz][qx][qy] and G_xz as [qy][qx][qz]: their tables contract the P axis first
+    S.G[3][qz * 9 + qx * 3 + qy] = sG * A12, S.G[4][qy * 9 + qx * 3 + qz] = sG * A13, S.G[5][lane] = sG * A23;
     // the qpoint origin + J xi (curfe.hpp:80), for the analytic load
     if (a.rkind == 1)
     {
@@ -318,12 +344,15 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
   double * const tUyz = S.tab + 648 + 972;
   if (needK)
   {
-    contract3(S.G[0], 6, cD, 6, cP, 6, cP, tSx, S.scr[0], S.scr[1], lane);
-    contract3(S.G[1], 6, cP, 6, cD, 6, cP, tSy, S.scr[0], S.scr[1], lane);
-    contract3(S.G[2], 6, cP, 6, cP, 6, cD, tSz, S.scr[0], S.scr[1], lane);
-    contract3(S.G[3], 9, cE, 9, cE, 6, cP, tUxy, S.scr[0], S.scr[1], lane); // [ex][ey][pz]
-    contract3(S.G[4], 9, cE, 6, cP, 9, cE, tUxz, S.scr[0], S.scr[1], lane); // [ex][py][ez]
-    contract3(S.G[5], 6, cP, 9, cE, 9, cE, tUyz, S.scr[0], S.scr[1], lane); // [px][ey][ez]
+    double const * const nP = S.coefN + 9;
+    double const * const nD = S.coefN + 27;
+    double const * const nE = S.coefN + 45;
+    contract3N(S.G[0], 6, nD, 6, nP, 6, nP, tSx, S.scr[0], S.scr[1], lane);  // [px][py][pz]
+    contract3N(S.G[1], 6, nP, 6, nD, 6, nP, tSy, S.scr[0], S.scr[1], lane);
+    contract3N(S.G[2], 6, nP, 6, nP, 6, nD, tSz, S.scr[0], S.scr[1], lane);
+    contract3N(S.G[3], 6, nP, 9, nE, 9, nE, tUxy, S.scr[0], S.scr[1], lane); // [pz][ex][ey]
+    contract3N(S.G[4], 6, nP, 9, nE, 9, nE, tUxz, S.scr[0], S.scr[1], lane); // [py][ex][ez]
+    contract3N(S.G[5], 6, nP, 9, nE, 9, nE, tUyz, S.scr[0], S.scr[1], lane); // [px][ey][ez]
   }
 
   // ---- entries i <= j and the scatter
@@ -339,12 +368,21 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
     double kv = 0., mv = 0.;
     if (needK)
     {
-      kv = tSx[px * 36 + py * 6 + pz] + tSy[px * 36 + py * 6 + pz];
-      kv += tSz[px * 36 + py * 6 + pz];
-      // the S tables share the index because D and P use the same symmetric classes
-      kv += tUxy[(3 * ix + jx) * 54 + (3 * jy + iy) * 6 + pz] + tUxy[(3 * jx + ix) * 54 + (3 * iy + jy) * 6 + pz];
-      kv += tUxz[(3 * ix + jx) * 54 + py * 9 + (3 * jz + iz)] + tUxz[(3 * jx + ix) * 54 + py * 9 + (3 * iz + jz)];
-      kv += tUyz[px * 81 + (3 * iy + jy) * 9 + (3 * jz + iz)] + tUyz[px * 81 + (3 * jy + iy) * 9 + (3 * iz + jz)];
+      // each table value times its deferred scale (gScale, in the layout of S.tab); the
+      // S tables share the index because D and P use the same symmetric classes
+      int const s = px * 36 + py * 6 + pz;
+      int const t[6] = {648 + pz * 81 + (3 * ix + jx) * 9 + (3 * jy + iy),
+                        648 + pz * 81 + (3 * jx + ix) * 9 + (3 * iy + jy),
+                        1134 + py * 81 + (3 * ix + jx) * 9 + (3 * jz + iz),
+                        1134 + py * 81 + (3 * jx + ix) * 9 + (3 * iz + jz),
+                        1620 + px * 81 + (3 * iy + jy) * 9 + (3 * jz + iz),
+                        1620 + px * 81 + (3 * jy + iy) * 9 + (3 * iz + jz)};
+      kv = tSx[s] * __ldg(gScale + s);
+      kv = fma(tSy[s], __ldg(gScale + 216 + s), kv);
+      kv = fma(tSz[s], __ldg(gScale + 432 + s), kv);
+#pragma unroll
+      for (int u = 0; u < 6; ++u)
+        kv = fma(S.tab[t[u]], __ldg(gScale + t[u]), kv);
     }
     if (needM)
       mv = S.Mt[px * 36 + py * 6 + pz];
@@ -442,7 +480,45 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
   for (int i = 0; i < N; ++i)
     for (int j = i; j < N; ++j)
       pairs.push_back((uint16_t)(i << 8 | j));
+  // the P, D, E classes divided by their first coefficient (the value at t_0, nonzero
+  // for every class), and the deferred scale of each stiffness table value: the
+  // product of its three classes' first coefficients, in the tables' layouts
+  std::vector<double> coefN(coef);
+  auto first = [&](int base, int cc) { return coef[base + 3 * cc]; };
+  for (int k = 9; k < 72; k += 3)
+    if (coef[k] == 0.)
+      return fail(c, PXG_ERR_UNSUPPORTED, "Q2 tables: a class vanishes at the first Gauss point");
+  for (int base : {9, 27})
+    for (int cc = 0; cc < 6; ++cc)
+      for (int k = 0; k < 3; ++k)
+        coefN[base + 3 * cc + k] = coef[base + 3 * cc + k] / first(base, cc);
+  for (int cc = 0; cc < 9; ++cc)
+    for (int k = 0; k < 3; ++k)
+      coefN[45 + 3 * cc + k] = coef[45 + 3 * cc + k] / first(45, cc);
+  std::vector<double> scale(3 * 216 + 3 * 486);
+  auto sP = [&](int cc) { return first(9, cc); };
+  auto sD = [&](int cc) { return first(27, cc); };
+  auto sE = [&](int cc) { return first(45, cc); };
+  for (int x = 0; x < 6; ++x)
+    for (int y = 0; y < 6; ++y)
+      for (int z = 0; z < 6; ++z)
+      {
+        int const k = x * 36 + y * 6 + z;
+        scale[k] = sD(x) * sP(y) * sP(z);
+        scale[216 + k] = sP(x) * sD(y) * sP(z);
+        scale[432 + k] = sP(x) * sP(y) * sD(z);
+      }
+  for (int p = 0; p < 6; ++p)
+    for (int e1 = 0; e1 < 9; ++e1)
+      for (int e2 = 0; e2 < 9; ++e2)
+      {
+        double const v = sP(p) * sE(e1) * sE(e2);
+        for (int tbl = 0; tbl < 3; ++tbl)
+          scale[648 + 486 * tbl + p * 81 + e1 * 9 + e2] = v;
+      }
   PXG_CUDA(c, cudaMemcpyToSymbol(gCoef, coef.data(), 72 * 8));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gCoefN, coefN.data(), 72 * 8));
+  PXG_CUDA(c, cudaMemcpyToSymbol(gScale, scale.data(), scale.size() * 8));
   PXG_CUDA(c, cudaMemcpyToSymbol(gT, t, 24));
   PXG_CUDA(c, cudaMemcpyToSymbol(gWl, wl, NQ * 8));
   PXG_CUDA(c, cudaMemcpyToSymbol(gRuleOfLat, ruleOfLat, NQ));
