@@ -20,7 +20,8 @@ kernel meets: FP64 instructions per second against the FMA rate measured live by
 pxg_fp64_rate), `dfl` (the same workload with the opt-in double-float kernels and
 their largest entrywise deviation from the FP64 result), `e2e.host` (the GPU's NUMA
 node and the CPUs the host-buffer leg ran on), `configs` (P1 16^3 x 6, P2 64^3 x 6,
-Q2 48^3), `adjoint` (Q1 96^3 gradient), `batched` (256 ragged problems, batched vs
+Q2 48^3; with P2, the L2 reduction rate its scatter meets, live from pxg_red_rate),
+`adjoint` (Q1 96^3 gradient), `batched` (256 ragged problems, batched vs
 one at a time) and `widened` (Dirichlet setup from facet markers, Taylor-Hood Stokes
 systems).
 """
@@ -289,6 +290,13 @@ def measure_configs(peak_gbs, reps=5):
                                                    L.Q2HEX: "kAssembleQ2"}[t]}
         del ctx, K, M, b
         torch.cuda.empty_cache()
+    # the L2 reduction rate the P2 scatter is bound by, live (pxg_red_rate, 32 MB array):
+    # one lane per 32-byte sector, as element-by-element reductions land, and four, as
+    # the warp-group scatter's sorted positions mostly do
+    r1, _ = L.red_rate(1)
+    r4, _ = L.red_rate(4)
+    out["p2tet_64"]["l2_red_per_s"] = {"lanes_per_sector_1": r1, "lanes_per_sector_4": r4,
+                                       "probe": "pxg_red_rate, 32 MB array"}
     return out
 
 

@@ -387,6 +387,14 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, const pxg_rhs_op 
  * chains; the ceiling of the FP64-bound element kernels, reported beside their time.
  * ms (may be NULL) receives the timed launch's duration. */
 pxg_status pxg_fp64_rate(int device, double * fma_per_s, double * ms);
+/* The rate of FP64 reductions (red.global.add.f64) on `device`, by lane pattern: every
+ * warp instruction adds into 32 doubles, `lanes_per_sector` (1, 2 or 4) consecutive
+ * lanes sharing one 32-byte sector, the sectors hashed over an array of `bytes` (a power
+ * of two, 4 KB .. 32 GB; below the 129 MB of L2 the array stays there).  Reductions per
+ * second of the best of three launches after a warm-up, and that launch's ms (optional).
+ * Measurement, beside pxg_fp64_rate: the bound of the element kernels' scatter.  No
+ * counterpart in proxpde. */
+pxg_status pxg_red_rate(int device, int lanes_per_sector, int64_t bytes, double * red_per_s, double * ms);
 
 /* ----------------------------------------------------- allocation-free prune
  * No counterpart in proxpde: an allocation-free variant of pxg_close_matrix's

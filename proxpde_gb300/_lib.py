@@ -35,7 +35,7 @@ EXPORTS = [
     "pxg_close_matrix", "pxg_interpolate", "pxg_prune_csr_noalloc",
     "pxg_cg", "pxg_adjoint_grad", "pxg_adjoint_forward", "pxg_adjoint_backward",
     "pxg_batch_set", "pxg_batch_adjoint", "pxg_device_alloc", "pxg_device_free", "pxg_memcpy",
-    "pxg_set_arithmetic", "pxg_fp64_rate", "pxg_sys_close_matrix", "pxg_get_qpoints",
+    "pxg_set_arithmetic", "pxg_fp64_rate", "pxg_red_rate", "pxg_sys_close_matrix", "pxg_get_qpoints",
 ]
 
 
@@ -117,6 +117,7 @@ def load(path: str = LIB_PATH):
         "pxg_set_scatter": ([vp, C.c_int, C.c_int], C.c_int),
         "pxg_set_arithmetic": ([vp, C.c_int], C.c_int),
         "pxg_fp64_rate": ([C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+        "pxg_red_rate": ([C.c_int, C.c_int, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "pxg_sys_create": ([C.POINTER(vp), vp, vp, vp, C.c_int, i64p, i64p], C.c_int),
         "pxg_sys_destroy": ([vp], C.c_int),
         "pxg_sys_get_pattern": ([vp, vp, vp], C.c_int),
@@ -163,6 +164,18 @@ def fp64_rate(device=0):
     st = L.pxg_fp64_rate(int(device), C.byref(r), C.byref(ms))
     if st:
         raise PxgError(st, "fp64_rate")
+    return r.value, ms.value
+
+
+def red_rate(lanes_per_sector, nbytes=32 << 20, device=0):
+    """(FP64 reductions per second, ms of the timed launch) measured on a device, with
+    lanes_per_sector (1, 2, 4) lanes of a warp adding into one 32-byte sector, over an
+    array of nbytes (a power of two)."""
+    L = load()
+    r, ms = C.c_double(), C.c_double()
+    st = L.pxg_red_rate(int(device), int(lanes_per_sector), int(nbytes), C.byref(r), C.byref(ms))
+    if st:
+        raise PxgError(st, "red_rate")
     return r.value, ms.value
 
 

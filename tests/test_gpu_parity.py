@@ -401,3 +401,20 @@ def test_fp64_rate_probe(engine):
     p = torch.cuda.get_device_properties(0)
     bound = p.multi_processor_count * 128 * 2.2e9
     assert 0 < rate < bound and ms > 0
+
+
+def test_red_rate_probe(engine):
+    """pxg_red_rate: FP64 reductions per second by lane pattern, on an L2-resident array
+    (32 MB) and a 1 GB one: positive, sectors shared by four lanes at least as fast per
+    reduction as one lane per sector (the scatter's design rests on it), and bad
+    arguments rejected."""
+    from proxpde_gb300._lib import PxgError, red_rate
+
+    for nbytes in (32 << 20, 1 << 30):
+        r1, ms1 = red_rate(1, nbytes)
+        r4, ms4 = red_rate(4, nbytes)
+        assert r1 > 0 and r4 > 0 and ms1 > 0 and ms4 > 0
+        assert r4 >= r1
+    for bad in ((3, 32 << 20), (1, 3 << 20), (1, 1024)):
+        with pytest.raises(PxgError):
+            red_rate(*bad)
