@@ -1235,6 +1235,18 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
               break;
             // the position's contributions in element order: no addition for the
             // first (the FP64 pipe is the scarce one)
+            // a position with few contributions: one reduction each (the L2 atomic unit
+            // has room, the FP64 pipe has not); more: sum them here, reduce once
+            if (b1[u] - b0[u] <= a.grpRedMax)
+            {
+              for (int k = b0[u]; k < b1[u]; ++k)
+              {
+                uint32_t const code = si[k];
+                red(op0.vals + pos[u], sw[((code >> 5) & 63u) * 32 + (code & 31u)]);
+                red(op1.vals + pos[u], sw[(55 + (code >> 11)) * 32 + (code & 31u)]);
+              }
+              continue;
+            }
             uint32_t code = si[b0[u]];
             double kk = sw[((code >> 5) & 63u) * 32 + (code & 31u)];
             double mm = sw[(55 + (code >> 11)) * 32 + (code & 31u)];
@@ -2214,6 +2226,7 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
           lg.grpPos = c->groups.pos.p;
           lg.grpBeg = c->groups.beg.p;
           lg.grpItem = c->groups.item.p;
+          lg.grpRedMax = c->groupRedMax;
         }
         // the warp-group scatter's shared memory favours small blocks (64 threads: ten
         // warps per SM), so that is its default

@@ -354,6 +354,9 @@ struct pxg_ctx
   bool q2Generic = false;
   // P2 FP64: sum each warp's contributions per distinct position before the reductions
   bool groupScatter = true;
+  // positions with at most this many contributions get one reduction per contribution
+  // (L2 adds them) instead of FP64 additions on the SM: 2 measured best at 64^3 x 6
+  int groupRedMax = 2;
   int sms = 0; // SMs of the device (persistent grids)
   // What produced each value array pxg_assemble wrote (its recipe): the lhs operators
   // added into it since it was last overwritten, with the versions of the coordinates,
@@ -430,6 +433,7 @@ struct AsmArgs
   int32_t const * grpPos;
   uint16_t const * grpBeg;
   uint16_t const * grpItem;
+  int grpRedMax;
 };
 
 // P2 tetrahedron local numbering (src/reffe.cpp:542-642): vertices 0-3, then the edges
