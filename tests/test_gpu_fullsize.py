@@ -1,7 +1,8 @@
 """Checks at the full sizes of the reference workloads:
 
 - entry by entry against the oracle (threaded over the host's cores): the Q1 128^3
-  K(k_e), M and sin3 load, and the P2 64^3 x 6 K(k_e) and M, each in the default FP64
+  K(k_e), M and sin3 load, the P2 64^3 x 6 K(k_e) and M, and the Q2 48^3 K(k_e), M
+  and sin3 load, each in the default FP64
   arithmetic and in the opt-in double-float one, with the normwise and entrywise
   tolerances of tests/helpers.py (1e-12 relative to each entry above the round-off
   floor of its row);
@@ -205,6 +206,33 @@ def test_p2_64_entrywise(engine, arith):
         csr, _ = O.build(O.P2TET, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=nt)
         compare_csr(g["mats"][m], csr, ndof, what=f"p2 64^3x6 {arith} {'KM'[m]}", eps=EPS_DFL if arith == "dfl" else EPS)
         del csr
+
+
+@pytest.mark.parametrize("arith", ["fp64", "dfl"])
+def test_q2_48_entrywise(engine, arith):
+    """The Q2 workload (perturbed Q2 48^3, K(k_e) + M + sin3 load: 110,592 elements,
+    57 M structural entries) entry by entry against the oracle: the DOF map, the pruned
+    CSR patterns and every value."""
+    from proxpde_gb300 import meshgen
+    from proxpde_gb300._lib import ARITH_DFL, ARITH_FP64
+
+    n = 48
+    xyz, conn = meshgen.cube_hex(n)
+    xyz = meshgen.perturb(xyz, n, 0.2, 20261209)
+    k = meshgen.lognormal(20261210, conn.shape[0], 1.0)
+    ops = [{"stiffness": 2, "stiff_coef": 1.0}, {"mass": 1, "mass_coef": 1.0}]
+    rhs = {"kind": 1, "fn": O.FN_SIN3, "coef": 1.0}
+    g = gpu_assemble(O.Q2HEX, xyz, conn, ops, rhs=rhs, k=k, arith=ARITH_DFL if arith == "dfl" else ARITH_FP64)
+    em, ndof = O.dofmap(O.Q2HEX, xyz.shape[0], conn)
+    assert ndof == g["ndof"] and np.array_equal(em, g["em"])
+    nt = _threads()
+    eps = EPS_DFL if arith == "dfl" else EPS
+    for m, op in enumerate(ops):
+        csr, _ = O.build(O.Q2HEX, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=nt)
+        compare_csr(g["mats"][m], csr, ndof, what=f"q2 48^3 {arith} {'KM'[m]}", eps=eps)
+        del csr
+    _, b = O.build(O.Q2HEX, xyz, conn, em, ndof, rhs={"kind": 1, "fn": O.FN_SIN3, "c": 1.0}, nthreads=nt)
+    assert_close(g["b"], b, what=f"q2 48^3 {arith} b", eps=eps)
 
 
 def test_q1_96_adjoint(engine):
