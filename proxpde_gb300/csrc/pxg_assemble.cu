@@ -2271,8 +2271,15 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
   {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     PXG_CUDA(c, cudaStreamIsCapturing(s, &cs));
-    if (cs == cudaStreamCaptureStatusNone && (st = buildScatterGroups(c)) != PXG_OK)
-      return st;
+    if (cs == cudaStreamCaptureStatusNone && buildScatterGroups(c) != PXG_OK)
+    {
+      // no room for the map (its build holds ~2.7 KB per element for a moment): this
+      // context adds its entries one by one, the same sums in another order
+      cudaGetLastError();
+      c->groups.reset();
+      c->groupScatter = false;
+      c->err.clear();
+    }
   }
   if (c->scatter == PXG_SCATTER_COLOUR)
   {
