@@ -83,6 +83,7 @@ struct BatchDev
   unsigned * bar; // [0] arrivals, [1] generation
   int * err;      // [0] barrier timeout
   unsigned extra; // arrivals expected beyond the grid (0; >0 only to test the timeout path)
+  int chunksPerBlock; // about this many chunks of rows per block and iteration
   double tol2;
   int maxIter;
   // problem table and the chunk tables of alternate iterations
@@ -333,9 +334,9 @@ __device__ __forceinline__ int blockExclusiveScan(int x, int & total)
 }
 
 // Block 0: cut the rows of the running problems into chunks of equal size (at least
-// 256 rows, about eight per block) for the iterations of parity `par`.  The chunks are
-// dealt round-robin to the blocks, so the work of an iteration follows the running
-// problems instead of a fixed row partition.
+// 256 rows, about d.chunksPerBlock = 4 per block) for the iterations of parity `par`.
+// The chunks are dealt round-robin to the blocks, so the work of an iteration follows
+// the running problems instead of a fixed row partition.
 __device__ void buildChunks(BatchDev const & d, int par)
 {
   __shared__ long long sRows;
@@ -349,7 +350,8 @@ __device__ void buildChunks(BatchDev const & d, int par)
   atomicAdd(reinterpret_cast<unsigned long long *>(&sRows), (unsigned long long)mine);
   __syncthreads();
   long long const rows = sRows;
-  long long csize = (rows + 8ll * gridDim.x - 1) / (8ll * gridDim.x);
+  long long const per = d.chunksPerBlock;
+  long long csize = (rows + per * gridDim.x - 1) / (per * gridDim.x);
   csize = csize < 256 ? 256 : csize;
   int running = 0;
   for (int base = 0; base < d.nprob; base += blockDim.x)
@@ -850,6 +852,10 @@ pxg_status pxg_batch_adjoint(pxg_ctx * const * ctxs, int nctx, pxg_rhs_op const 
     // than the grid has, so the bounded waits run out (tests of the timeout path)
     char const * t = getenv("PXG_TEST_BARRIER_SHORTFALL");
     d.extra = (t && t[0] == '1') ? 1u : 0u;
+    // chunks per block and iteration: 4 measured best on the 256-problem batch (2: 410,
+    // 4: 361, 8: 368, 16: 411 ms); PXG_BATCH_CHUNKS overrides
+    char const * cpb = getenv("PXG_BATCH_CHUNKS");
+    d.chunksPerBlock = (cpb && atoi(cpb) > 0) ? atoi(cpb) : 4;
   }
 
   int dev = c0->device, sms = 0, perSm = 0;
