@@ -326,16 +326,25 @@ def measure_adjoint(n=96, reps=2):
             "cg_iters": {"forward": P.iters[0], "adjoint": P.iters[1]}, "rtol": 1e-10}
 
 
-def measure_batched(n_hex=128, n_tet=128, reps=3, tune=True):
+def measure_batched(n_hex=128, n_tet=128, reps=3, tune=True, rank=0, world=1, dev="cuda"):
     """Batched adjoint gradients of 256 ragged problems (n ~ U{8..48}); batched persistent graph vs the
-    same problems one at a time through the plain forward/backward pair."""
+    same problems one at a time through the plain forward/backward pair.  On several ranks
+    (one GPU each) the problems are split between them (batch.shard: independent problems,
+    no exchange) and each time is the largest over the ranks."""
     import torch
 
     from proxpde_gb300 import batch
     from proxpde_gb300.adjoint import DiffusionLoss, DiffusionProblem
 
-    probs = batch.make_problems(n_hex=n_hex, n_tet=n_tet)
-    groups = [batch.Batch([p for p in probs if p["etype"] == 2]), batch.Batch([p for p in probs if p["etype"] == 0])]
+    sizes = batch.problem_sizes(n_hex=n_hex, n_tet=n_tet)
+    mine = batch.shard(sizes, n_hex, rank, world)
+    probs = batch.make_problems(n_hex=n_hex, n_tet=n_tet, only=mine)
+    groups = [batch.Batch(ps) for ps in ([p for p in probs if p["etype"] == 2], [p for p in probs if p["etype"] == 0])
+              if ps]
+
+    def job_time(t):
+        return max_over_ranks(t, world, dev)
+
     # the autotuner picks each batch's element kernel (elements per CTA, scatter)
     tuning = [g.ctx.autotune(op0={"stiffness": 2, "stiff_coef": 1.0, "apply_bc": 1}, op1={"mass": 1, "mass_coef": 1.0},
                              rhs={"kind": 1, "fn": 0, "coef": 1.0, "apply_bc": 1}) for g in groups] if tune else None
@@ -343,10 +352,11 @@ def measure_batched(n_hex=128, n_tet=128, reps=3, tune=True):
     torch.cuda.synchronize()
     ts = []
     for _ in range(reps):
+        barrier(world)
         t0 = time.perf_counter()
         losses, iters = batch.batch_adjoint(groups)
         torch.cuda.synchronize()
-        ts.append(time.perf_counter() - t0)
+        ts.append(job_time(time.perf_counter() - t0))
     tb = min(ts)
     # sequential plain launches
     plain = []
@@ -363,9 +373,10 @@ def measure_batched(n_hex=128, n_tet=128, reps=3, tune=True):
         torch.cuda.synchronize()
         return out
     seq_pass()
+    barrier(world)
     t0 = time.perf_counter()
     gs = seq_pass()
-    ts_ = time.perf_counter() - t0
+    ts_ = job_time(time.perf_counter() - t0)
     # batched vs plain gradients
     err = 0.0
     i = 0
@@ -374,8 +385,12 @@ def measure_batched(n_hex=128, n_tet=128, reps=3, tune=True):
             a, b = g.grad_of(q), gs[i]
             err = max(err, float(torch.linalg.norm(a - b) / torch.linalg.norm(b)))
             i += 1
-    E = sum(g.nelem for g in groups)
+    err = job_time(err)
+    E = int(job_sum(sum(g.nelem for g in groups), world, dev))
+    iters = int(job_time(iters))
     return {"workload": f"{n_hex} Q1-hex + {n_tet} P1-tet cubes, n~U{{8..48}}, K+M assembly + adjoint gradient",
+            "ranks": world, "partition": "problems split over the ranks (largest first to the least loaded), "
+            "no exchange" if world > 1 else "one rank",
             "problems": n_hex + n_tet, "elements": E, "batched_grads_per_s": (n_hex + n_tet) / tb,
             "sequential_grads_per_s": (n_hex + n_tet) / ts_, "speedup": ts_ / tb, "batched_ms": 1e3 * tb,
             "sequential_ms": 1e3 * ts_, "max_cg_iters": iters,
@@ -402,9 +417,28 @@ def max_over_ranks(x, world, device):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([float(x)], device=device)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return t.item()
+
+
+def job_sum(x, world, device):
+    """The sum of the ranks' values (no-op on one rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return t.item()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
 
 
 def run_reference(args, world, rank):
@@ -669,14 +703,16 @@ def main():
                "value_1thread": v_one, "sample_1thread": f"{min(args.cpu_n, 24)}^3 hexes, 1 thread"}
 
     adjoint = batched = widened = configs = None
+    if not args.no_batched:
+        # every rank: the batch's problems are split over the ranks
+        barrier(world)
+        batched = measure_batched(tune=not args.no_tune, rank=rank, world=world, dev=dev)
     if rank == 0 and not args.no_widened:
         widened = measure_widened(xyz, conn)
     if rank == 0 and not args.no_configs:
         configs = measure_configs(hbm)
     if rank == 0 and not args.no_adjoint:
         adjoint = measure_adjoint()
-    if rank == 0 and not args.no_batched:
-        batched = measure_batched(tune=not args.no_tune)
 
     if rank == 0:
         line = {

@@ -17,12 +17,38 @@ from . import meshgen
 from ._lib import FN_CONST, FN_SIN3, P1TET, Q1HEX, Context, PxgError, RhsOp, _ptr
 
 
-def make_problems(n_hex=128, n_tet=128, nmin=8, nmax=48, alpha=0.2, seed=20261209):
+def problem_sizes(n_hex=128, n_tet=128, nmin=8, nmax=48, seed=20261209):
+    """The seeded cube size n ~ U{nmin..nmax} of every problem (hexahedra first)."""
+    return nmin + (meshgen.splitmix64(seed, np.arange(n_hex + n_tet)) % np.uint64(nmax - nmin + 1)).astype(np.int64)
+
+
+def shard(sizes, n_hex, rank, world):
+    """The problems of `rank` when a batch is split over `world` ranks (one GPU each):
+    independent problems, so no exchange between the ranks.  Largest first, each to
+    the rank with the least work so far; the work of a problem is its nonzeros (27 per
+    row for Q1 hexahedra, 15 for P1 tetrahedra, (n + 1)^3 rows) times n, as the CG
+    iterations grow with n.  Returns ascending problem indices."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    cost = np.where(np.arange(sizes.size) < n_hex, 27.0, 15.0) * (sizes + 1.0) ** 3 * sizes
+    load = np.zeros(world)
+    owner = np.empty(sizes.size, dtype=np.int64)
+    for p in sorted(range(sizes.size), key=lambda q: (-cost[q], q)):
+        r = int(np.argmin(load))
+        owner[p] = r
+        load[r] += cost[p]
+    return np.nonzero(owner == rank)[0]
+
+
+def make_problems(n_hex=128, n_tet=128, nmin=8, nmax=48, alpha=0.2, seed=20261209, only=None):
     """Seeded problems: cube sizes n ~ U{nmin..nmax}; Q1 hexahedra first, then P1
-    tetrahedra (6 per cube); nodes perturbed by U(-alpha h, alpha h); k_e = exp(N(0,1))."""
-    sizes = nmin + (meshgen.splitmix64(seed, np.arange(n_hex + n_tet)) % np.uint64(nmax - nmin + 1)).astype(np.int64)
+    tetrahedra (6 per cube); nodes perturbed by U(-alpha h, alpha h); k_e = exp(N(0,1)).
+    `only`: the indices of the problems to build (a rank's shard), default all."""
+    sizes = problem_sizes(n_hex, n_tet, nmin, nmax, seed)
+    keep = set(range(sizes.size)) if only is None else {int(q) for q in only}
     probs = []
     for p, n in enumerate(sizes.tolist()):
+        if p not in keep:
+            continue
         hexa = p < n_hex
         xyz, conn = meshgen.cube_hex(n) if hexa else meshgen.cube_tet6(n)
         xyz = meshgen.perturb(xyz, n, alpha, seed + 1 + 7 * p)
