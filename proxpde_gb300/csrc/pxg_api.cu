@@ -129,6 +129,7 @@ pxg_status pxg_create(pxg_ctx ** out, int device)
   c->tetGeneric = envOn("PXG_TET_GENERIC");
   c->q2Generic = envOn("PXG_Q2_GENERIC");
   c->groupScatter = !envOn("PXG_NO_GROUP_SCATTER");
+  c->zeroOverlap = !envOn("PXG_NO_ZERO_OVERLAP");
   if (char const * r = getenv("PXG_GROUP_RED_MAX"))
     c->groupRedMax = atoi(r);
   pxg_status s = ensureDevice(c);

@@ -1187,6 +1187,8 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
 #pragma unroll
       for (int c = 0; c < 7; ++c)
         mc[c] = am * MHAT<T>(p2MassRepI(c), p2MassRepJ(c));
+      if (!grouped)
+        pdlWait(); // the writes start here (the grouped path waits before its flush)
       if (a.grpOff)
       {
         // warp-group scatter: the lane's values and the group's contribution codes to
@@ -1214,6 +1216,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
         for (int k = lane; k < (nItems + 7) / 8; k += W)
           reinterpret_cast<uint4 *>(si)[k] = gi[k];
         __syncwarp(mask);
+        pdlWait(); // the writes start here
         int32_t const dEnd = a.grpOff[g + 1];
         constexpr int U = 4;
         for (int32_t d0 = a.grpOff[g]; d0 < dEnd; d0 += U * W)
@@ -1279,6 +1282,7 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
       goto entriesDone;
     }
   }
+  pdlWait(); // the writes start here
 #pragma unroll kRowUnroll
   for (int i = 0; i < N; ++i)
   {
@@ -1970,7 +1974,8 @@ void launchAssembleTet64(AsmArgs const & a, cudaStream_t s, int threads)
       smem = (size_t)(nt / 32) * kP2GroupSmemPerWarp;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
-    kern<<<blocks, nt, smem, s>>>(a);
+    if (blocks > 0)
+      launchElemKernel(kern, blocks, nt, smem, s, a);
   };
   if (threads == 64)
     return go(kAssembleTet64<T, 64>, 64);
@@ -2027,6 +2032,23 @@ void recordRecipe(pxg_ctx * c, double const * vals, pxg_lhs_op const & o, bool a
     R.valid = false;
   else
     R.ops.push_back(pxg_ctx::LhsRec{o.stiffness, o.mass, o.apply_bc, o.stiff_coef, o.mass_coef});
+}
+
+// zero the outputs of an assembly (z0, z1: n values; zb: nb), letting the element kernel
+// that follows start at once as its programmatic dependent (pdlWait)
+__global__ void __launch_bounds__(256) kZeroOutputs(double * z0, double * z1, int64_t n, double * zb, int64_t nb)
+{
+  asm volatile("griddepcontrol.launch_dependents;");
+  int64_t const nthr = (int64_t)gridDim.x * blockDim.x, t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t k = t; k < n; k += nthr)
+  {
+    if (z0)
+      z0[k] = 0.;
+    if (z1)
+      z1[k] = 0.;
+  }
+  for (int64_t k = t; k < nb; k += nthr)
+    zb[k] = 0.;
 }
 
 // the element lists of every DOF, ascending (built once per DOF map)
@@ -2175,11 +2197,34 @@ pxg_status pxg_assemble(pxg_ctx * c, pxg_lhs_op const * op0, double * vals0, pxg
       recordRecipe(c, outs[m], *ops[m], (flags & PXG_ACCUMULATE) != 0);
   if (!(flags & PXG_ACCUMULATE))
   {
-    for (int m = 0; m < 2; ++m)
-      if (a.op[m].on)
-        PXG_CUDA(c, cudaMemsetAsync(a.op[m].vals, 0, (size_t)c->nnz * 8, s));
-    if (b)
-      PXG_CUDA(c, cudaMemsetAsync(b, 0, (size_t)c->ndof * 8, s));
+    // the default FP64 element kernels in element order, outside a stream capture: a
+    // zeroing kernel that the element kernel overlaps (its blocks compute while the
+    // outputs are zeroed, and wait before they write); otherwise memsets.  Measured
+    // against the memsets: P1 16^3 x 6 0.033 -> 0.025 ms (one launch fewer), Q1 128^3
+    // 5.14 -> 5.13 ms, Q2 48^3 equal; P2 64^3 x 6 1.41 -> 1.43 ms, so P2 keeps memsets
+    bool const fp64 = c->arith == PXG_ARITH_FP64;
+    bool const pdlOk = fp64 && c->zeroOverlap && c->scatter == PXG_SCATTER_REDUCE &&
+                       ((c->etype == Q1HEX && !c->q1Generic && !c->q1Thread && !c->q1Group) ||
+                        (c->etype == P1TET && !c->tetGeneric) || (c->etype == Q2HEX && !c->q2Generic));
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (pdlOk)
+      PXG_CUDA(c, cudaStreamIsCapturing(s, &cs));
+    if (pdlOk && cs == cudaStreamCaptureStatusNone)
+    {
+      kZeroOutputs<<<(unsigned)(2 * c->sms), 256, 0, s>>>(a.op[0].on ? a.op[0].vals : nullptr,
+                                                          a.op[1].on ? a.op[1].vals : nullptr, c->nnz, b,
+                                                          b ? c->ndof : 0);
+      PXG_CUDA(c, cudaGetLastError());
+      a.pdl = 1;
+    }
+    else
+    {
+      for (int m = 0; m < 2; ++m)
+        if (a.op[m].on)
+          PXG_CUDA(c, cudaMemsetAsync(a.op[m].vals, 0, (size_t)c->nnz * 8, s));
+      if (b)
+        PXG_CUDA(c, cudaMemsetAsync(b, 0, (size_t)c->ndof * 8, s));
+    }
   }
   // rhs kind 3 (values at the quadrature points) runs in the per-quadrature-point FP64
   // kernel, after the element kernel has done the matrices and their BC lifts

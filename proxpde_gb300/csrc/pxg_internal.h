@@ -354,6 +354,8 @@ struct pxg_ctx
   bool q2Generic = false;
   // P2 FP64: sum each warp's contributions per distinct position before the reductions
   bool groupScatter = true;
+  // zero the outputs with a kernel that the FP64 element kernel overlaps (else memsets)
+  bool zeroOverlap = true;
   // positions with at most this many contributions get one reduction per contribution
   // (L2 adds them) instead of FP64 additions on the SM: 2 measured best at 64^3 x 6
   int groupRedMax = 2;
@@ -434,7 +436,34 @@ struct AsmArgs
   uint16_t const * grpBeg;
   uint16_t const * grpItem;
   int grpRedMax;
+  // launched as a programmatic dependent of the zeroing of its outputs (pdlWait)
+  int pdl;
 };
+
+// The default FP64 element kernels run as programmatic dependents of the kernel that
+// zeroes their outputs: their blocks start while the (DRAM-bound) zeroing runs, compute
+// their element values, and wait for it only before their first write.  On a plain
+// launch the wait returns at once.
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// launch an element kernel, as a programmatic dependent of the stream's previous
+// launch when a.pdl is set
+template <typename Kern>
+inline cudaError_t launchElemKernel(Kern kern, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                                    AsmArgs const & a)
+{
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = a.pdl ? at : nullptr;
+  cfg.numAttrs = a.pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, a);
+}
 
 // P2 tetrahedron local numbering (src/reffe.cpp:542-642): vertices 0-3, then the edges
 // 01 12 20 03 13 23 as nodes 4-9; end k of edge node n

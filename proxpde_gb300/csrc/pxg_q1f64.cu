@@ -392,6 +392,7 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
 
   // ---- 5. load vector (buildLhs' BC values and buildRhs), before the tables so that
   // the offsets die early
+  pdlWait(); // the writes start here
   bool const bcOps = (op0.on && op0.bc) || (op1.on && op1.bc);
   if (a.b && cons && bcOps)
   {
@@ -792,10 +793,12 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
 
 void launchAssembleQ1F64(AsmArgs const & a, cudaStream_t s, int threads)
 {
+  if (a.nelem <= 0)
+    return;
   if (threads == 64)
-    kAssembleQ1F64<64, 6><<<(unsigned)((a.nelem + 63) / 64), 64, 0, s>>>(a);
+    launchElemKernel(kAssembleQ1F64<64, 6>, (unsigned)((a.nelem + 63) / 64), 64, 0, s, a);
   else
-    kAssembleQ1F64<128, 1><<<(unsigned)((a.nelem + 127) / 128), 128, 0, s>>>(a);
+    launchElemKernel(kAssembleQ1F64<128, 1>, (unsigned)((a.nelem + 127) / 128), 128, 0, s, a);
 }
 
 } // namespace pxg

@@ -276,7 +276,8 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
   double const * const cD = S.coef + 27;
   double const * const cE = S.coef + 45;
 
-  // ---- load vector (buildLhs' BC values, buildRhs)
+  // ---- load vector (buildLhs' BC values, buildRhs); the writes start here
+  pdlWait();
   bool const bcOps = (op0.on && op0.bc) || (op1.on && op1.bc);
   if (a.b && cons && bcOps && lane < N && ((cons >> lane) & 1u))
   {
@@ -531,7 +532,7 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
 void launchAssembleQ2F64(AsmArgs const & a, cudaStream_t s)
 {
   if (a.nelem > 0)
-    kAssembleQ2F64<<<(unsigned)a.nelem, 32, 0, s>>>(a);
+    launchElemKernel(kAssembleQ2F64, (unsigned)a.nelem, 32, 0, s, a);
 }
 
 } // namespace pxg
