@@ -727,7 +727,9 @@ def main():
                        "setup_s": setup_s, "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "dfl": dfl, "widened": widened,
             "configs": configs,
-            "gpu_launches": 3 * args.steps, "adjoint": adjoint, "batched": batched,
+            # per step: the zeroing of K, M and b (kZeroOutputs), the assembly (kAssembleQ1F64)
+            # and the two prune counts (kPruneCount)
+            "gpu_launches": 4 * args.steps, "adjoint": adjoint, "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
