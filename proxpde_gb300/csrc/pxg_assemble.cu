@@ -2034,6 +2034,8 @@ void recordRecipe(pxg_ctx * c, double const * vals, pxg_lhs_op const & o, bool a
     R.ops.push_back(pxg_ctx::LhsRec{o.stiffness, o.mass, o.apply_bc, o.stiff_coef, o.mass_coef});
 }
 
+namespace pxg
+{
 // zero the outputs of an assembly (z0, z1: n values; zb: nb), letting the element kernel
 // that follows start at once as its programmatic dependent (pdlWait)
 __global__ void __launch_bounds__(256) kZeroOutputs(double * z0, double * z1, int64_t n, double * zb, int64_t nb)
@@ -2050,6 +2052,7 @@ __global__ void __launch_bounds__(256) kZeroOutputs(double * z0, double * z1, in
   for (int64_t k = t; k < nb; k += nthr)
     zb[k] = 0.;
 }
+} // namespace pxg
 
 // the element lists of every DOF, ascending (built once per DOF map)
 pxg_status ensureDofElem(pxg_ctx * c)
