@@ -50,6 +50,11 @@ __device__ uint8_t gRuleOfLat[NQ]; // the rule's point index of each lattice poi
 __device__ uint8_t gLatOfNode[N];  // node n -> ax * 9 + ay * 3 + az (1D function indices)
 __device__ uint8_t gNodeOfLat[N];
 __device__ uint16_t gPairsF[NP];   // (i << 8 | j), i <= j
+// per pair, its index into each table (the layouts of the contractions below): the S
+// tables' (shared by the mass and S_x, S_y, S_z), then U_xy, U_xy transposed, U_xz,
+// U_xz transposed, U_yz, U_yz transposed; 8 per pair (one padding)
+__device__ uint16_t gPairIdx[NP * 8];
+constexpr int kPairsPerLane = (NP + 31) / 32; // 12
 
 constexpr int kTab = 3 * 216 + 3 * 486; // S_x S_y S_z U_xy U_xz U_yz
 
@@ -146,8 +151,7 @@ struct Smem
   double H[8][3]; // Walsh-Hadamard transform of the vertices, [kx + 2 ky + 4 kz][r]
   double G[6][NQ];
   double ad[NQ];
-  double Mt[216];
-  double tab[kTab];
+  double tab[486]; // one table at a time: the mass, then S_x, S_y, S_z, U_xy, U_xz, U_yz
   double scr[2][243];
   double bv[N];
   uint32_t dof[N];
@@ -326,67 +330,76 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
     __syncwarp();
   }
 
-  // ---- mass table: w |det J| (times a single mass operator's coefficient, and the
-  // 1/512) contracted with P over the three axes
+  // ---- the tables one at a time into S.tab, each lane adding them into the entries
+  // of its pairs p = lane + 32 k (kv, mv in registers): the mass table w |det J| (times
+  // a single mass operator's coefficient, and the 1/512) contracted with P over the
+  // three axes, then the six stiffness tables (normalised stages; each value times its
+  // deferred scale, gScale in the tables' concatenated layout)
+  double kv[kPairsPerLane], mv[kPairsPerLane];
+#pragma unroll
+  for (int k = 0; k < kPairsPerLane; ++k)
+    kv[k] = 0., mv[k] = 0.;
+  auto addTable = [&](int slot0, int slot1, int scaleBase, bool toMass) {
+#pragma unroll
+    for (int k = 0; k < kPairsPerLane; ++k)
+    {
+      int const p = lane + 32 * k;
+      if (p >= NP)
+        break;
+      int const t0 = gPairIdx[8 * p + slot0];
+      if (toMass)
+        mv[k] = S.tab[t0];
+      else
+      {
+        kv[k] = fma(S.tab[t0], __ldg(gScale + scaleBase + t0), kv[k]);
+        if (slot1 >= 0)
+        {
+          int const t1 = gPairIdx[8 * p + slot1];
+          kv[k] = fma(S.tab[t1], __ldg(gScale + scaleBase + t1), kv[k]);
+        }
+      }
+    }
+    __syncwarp(); // before the next table overwrites S.tab
+  };
   if (needM)
   {
     double const mcf = (foldM ? (m0 ? ms0 : ms1) : 1.0) * (1. / 512.);
     if (lane < NQ)
       S.scr[1][lane] = mcf * S.ad[lane];
     __syncwarp();
-    contract3(S.scr[1], 6, cP, 6, cP, 6, cP, S.Mt, S.scr[0], S.tab, lane);
+    contract3(S.scr[1], 6, cP, 6, cP, 6, cP, S.tab, S.scr[0], S.scr[1], lane);
+    addTable(0, -1, 0, true);
   }
-  // ---- stiffness tables
-  double * const tSx = S.tab;
-  double * const tSy = S.tab + 216;
-  double * const tSz = S.tab + 432;
-  double * const tUxy = S.tab + 648;
-  double * const tUxz = S.tab + 648 + 486;
-  double * const tUyz = S.tab + 648 + 972;
   if (needK)
   {
     double const * const nP = S.coefN + 9;
     double const * const nD = S.coefN + 27;
     double const * const nE = S.coefN + 45;
-    contract3N(S.G[0], 6, nD, 6, nP, 6, nP, tSx, S.scr[0], S.scr[1], lane);  // [px][py][pz]
-    contract3N(S.G[1], 6, nP, 6, nD, 6, nP, tSy, S.scr[0], S.scr[1], lane);
-    contract3N(S.G[2], 6, nP, 6, nP, 6, nD, tSz, S.scr[0], S.scr[1], lane);
-    contract3N(S.G[3], 6, nP, 9, nE, 9, nE, tUxy, S.scr[0], S.scr[1], lane); // [pz][ex][ey]
-    contract3N(S.G[4], 6, nP, 9, nE, 9, nE, tUxz, S.scr[0], S.scr[1], lane); // [py][ex][ez]
-    contract3N(S.G[5], 6, nP, 9, nE, 9, nE, tUyz, S.scr[0], S.scr[1], lane); // [px][ey][ez]
+    contract3N(S.G[0], 6, nD, 6, nP, 6, nP, S.tab, S.scr[0], S.scr[1], lane); // [px][py][pz]
+    addTable(0, -1, 0, false);
+    contract3N(S.G[1], 6, nP, 6, nD, 6, nP, S.tab, S.scr[0], S.scr[1], lane);
+    addTable(0, -1, 216, false);
+    contract3N(S.G[2], 6, nP, 6, nP, 6, nD, S.tab, S.scr[0], S.scr[1], lane);
+    addTable(0, -1, 432, false);
+    contract3N(S.G[3], 6, nP, 9, nE, 9, nE, S.tab, S.scr[0], S.scr[1], lane); // [pz][ex][ey]
+    addTable(1, 2, 648, false);
+    contract3N(S.G[4], 6, nP, 9, nE, 9, nE, S.tab, S.scr[0], S.scr[1], lane); // [py][ex][ez]
+    addTable(3, 4, 1134, false);
+    contract3N(S.G[5], 6, nP, 9, nE, 9, nE, S.tab, S.scr[0], S.scr[1], lane); // [px][ey][ez]
+    addTable(5, 6, 1620, false);
   }
 
-  // ---- entries i <= j and the scatter
+  // ---- the scatter of the entries i <= j
   uint16_t const * rk = a.rank + e * (int64_t)(N * N);
   bool const anyBc = cons && bcOps;
-  for (int p = lane; p < NP; p += 32)
+#pragma unroll
+  for (int k = 0; k < kPairsPerLane; ++k)
   {
+    int const p = lane + 32 * k;
+    if (p >= NP)
+      break;
     uint16_t const pr = gPairsF[p];
     int const i = pr >> 8, j = pr & 0xff;
-    int const Li = S.latOfNode[i], Lj = S.latOfNode[j];
-    int const ix = Li / 9, iy = (Li / 3) % 3, iz = Li % 3, jx = Lj / 9, jy = (Lj / 3) % 3, jz = Lj % 3;
-    int const px = symCls(ix, jx), py = symCls(iy, jy), pz = symCls(iz, jz);
-    double kv = 0., mv = 0.;
-    if (needK)
-    {
-      // each table value times its deferred scale (gScale, in the layout of S.tab); the
-      // S tables share the index because D and P use the same symmetric classes
-      int const s = px * 36 + py * 6 + pz;
-      int const t[6] = {648 + pz * 81 + (3 * ix + jx) * 9 + (3 * jy + iy),
-                        648 + pz * 81 + (3 * jx + ix) * 9 + (3 * iy + jy),
-                        1134 + py * 81 + (3 * ix + jx) * 9 + (3 * jz + iz),
-                        1134 + py * 81 + (3 * jx + ix) * 9 + (3 * iz + jz),
-                        1620 + px * 81 + (3 * iy + jy) * 9 + (3 * jz + iz),
-                        1620 + px * 81 + (3 * jy + iy) * 9 + (3 * iz + jz)};
-      kv = tSx[s] * __ldg(gScale + s);
-      kv = fma(tSy[s], __ldg(gScale + 216 + s), kv);
-      kv = fma(tSz[s], __ldg(gScale + 432 + s), kv);
-#pragma unroll
-      for (int u = 0; u < 6; ++u)
-        kv = fma(S.tab[t[u]], __ldg(gScale + t[u]), kv);
-    }
-    if (needM)
-      mv = S.Mt[px * 36 + py * 6 + pz];
     int32_t const pij = S.rp[i] + rk[i * N + j], pji = S.rp[j] + rk[j * N + i];
     bool const ci = (cons >> i) & 1u, cj = (cons >> j) & 1u;
 #pragma unroll
@@ -398,12 +411,12 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
       double val;
       if (op.stiff)
       {
-        val = foldK ? kv : (m ? ks1 : ks0) * kv;
+        val = foldK ? kv[k] : (m ? ks1 : ks0) * kv[k];
         if (op.mass)
-          val = foldM ? val + mv : fma(m ? ms1 : ms0, mv, val);
+          val = foldM ? val + mv[k] : fma(m ? ms1 : ms0, mv[k], val);
       }
       else
-        val = foldM ? mv : (m ? ms1 : ms0) * mv;
+        val = foldM ? mv[k] : (m ? ms1 : ms0) * mv[k];
       if (anyBc && op.bc && (ci || cj))
       {
         condenseF(op.vals + pij, a.bcDiag, a.b, S.dof[i], S.dof[j], S.bv[i], S.bv[j], ci, cj, i == j, val);
@@ -526,6 +539,26 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
   PXG_CUDA(c, cudaMemcpyToSymbol(gLatOfNode, latOfNode, N));
   PXG_CUDA(c, cudaMemcpyToSymbol(gNodeOfLat, nodeOfLat, N));
   PXG_CUDA(c, cudaMemcpyToSymbol(gPairsF, pairs.data(), pairs.size() * 2));
+  // each pair's index into the tables: S (and mass) [px][py][pz]; U_xy [pz][ex][ey],
+  // U_xz [py][ex][ez], U_yz [px][ey][ez] with E classes 3a + b of l'_a l_b (the
+  // derivative's axis first), and their transposed terms
+  std::vector<uint16_t> pidx(pairs.size() * 8, 0);
+  for (size_t q = 0; q < pairs.size(); ++q)
+  {
+    int const i = pairs[q] >> 8, j = pairs[q] & 0xff;
+    int const Li = latOfNode[i], Lj = latOfNode[j];
+    int const ix = Li / 9, iy = (Li / 3) % 3, iz = Li % 3, jx = Lj / 9, jy = (Lj / 3) % 3, jz = Lj % 3;
+    int const px = symCls(ix, jx), py = symCls(iy, jy), pz = symCls(iz, jz);
+    uint16_t * const o = &pidx[8 * q];
+    o[0] = (uint16_t)(px * 36 + py * 6 + pz);
+    o[1] = (uint16_t)(pz * 81 + (3 * ix + jx) * 9 + (3 * jy + iy));
+    o[2] = (uint16_t)(pz * 81 + (3 * jx + ix) * 9 + (3 * iy + jy));
+    o[3] = (uint16_t)(py * 81 + (3 * ix + jx) * 9 + (3 * jz + iz));
+    o[4] = (uint16_t)(py * 81 + (3 * jx + ix) * 9 + (3 * iz + jz));
+    o[5] = (uint16_t)(px * 81 + (3 * iy + jy) * 9 + (3 * jz + iz));
+    o[6] = (uint16_t)(px * 81 + (3 * jy + iy) * 9 + (3 * iz + jz));
+  }
+  PXG_CUDA(c, cudaMemcpyToSymbol(gPairIdx, pidx.data(), pidx.size() * 2));
   return PXG_OK;
 }
 
