@@ -1199,13 +1199,17 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
         unsigned char * const wbase = reinterpret_cast<unsigned char *>(gsm) + (threadIdx.x >> 5) * kP2GroupSmemPerWarp;
         double * const sw = reinterpret_cast<double *>(wbase);
         uint16_t * const si = reinterpret_cast<uint16_t *>(wbase + kP2GroupValues * 32 * sizeof(double));
+        // value v of lane l at v * 32 + (l ^ (v & 15)): the flush reads, in one
+        // instruction, values of the same few elements (lanes) for different entries,
+        // which this swizzle spreads over the banks
+        auto swAt = [sw](uint32_t v, uint32_t l) -> double & { return sw[v * 32 + (l ^ (v & 15u))]; };
         p2ForPairs<0, 0>([&](auto I, auto J) {
           constexpr int i = decltype(I)::value, j = decltype(J)::value;
-          sw[p2UpperIdx(i, j) * 32 + lane] = p2Stiff<i, j>(s);
+          swAt(p2UpperIdx(i, j), lane) = p2Stiff<i, j>(s);
         });
 #pragma unroll
         for (int c = 0; c < 7; ++c)
-          sw[(55 + c) * 32 + lane] = mc[c];
+          swAt(55 + c, lane) = mc[c];
         unsigned const mask = __activemask();
         int const W = __popc(mask); // the active lanes are 0 .. W - 1
         int64_t const g = e >> 5;
@@ -1245,19 +1249,19 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
               for (int k = b0[u]; k < b1[u]; ++k)
               {
                 uint32_t const code = si[k];
-                red(op0.vals + pos[u], sw[((code >> 5) & 63u) * 32 + (code & 31u)]);
-                red(op1.vals + pos[u], sw[(55 + (code >> 11)) * 32 + (code & 31u)]);
+                red(op0.vals + pos[u], swAt((code >> 5) & 63u, code & 31u));
+                red(op1.vals + pos[u], swAt(55 + (code >> 11), code & 31u));
               }
               continue;
             }
             uint32_t code = si[b0[u]];
-            double kk = sw[((code >> 5) & 63u) * 32 + (code & 31u)];
-            double mm = sw[(55 + (code >> 11)) * 32 + (code & 31u)];
+            double kk = swAt((code >> 5) & 63u, code & 31u);
+            double mm = swAt(55 + (code >> 11), code & 31u);
             for (int k = b0[u] + 1; k < b1[u]; ++k)
             {
               code = si[k];
-              kk += sw[((code >> 5) & 63u) * 32 + (code & 31u)];
-              mm += sw[(55 + (code >> 11)) * 32 + (code & 31u)];
+              kk += swAt((code >> 5) & 63u, code & 31u);
+              mm += swAt(55 + (code >> 11), code & 31u);
             }
             red(op0.vals + pos[u], kk);
             red(op1.vals + pos[u], mm);
