@@ -1225,28 +1225,61 @@ __global__ void __launch_bounds__(NT) kAssembleTet64(AsmArgs a)
         unsigned const mask = __activemask();
         int const W = __popc(mask); // the active lanes are 0 .. W - 1
         int64_t const g = e >> 5;
-        // the group's codes: W * 100 of them, 16 bytes (8 codes) per load; the map pads
-        // the last group's codes to a multiple of 8
         int const nItems = W * 100;
-        uint4 const * const gi = reinterpret_cast<uint4 const *>(a.grpItem + g * kP2GroupItems);
-        for (int k = lane; k < (nItems + 7) / 8; k += W)
-          reinterpret_cast<uint4 *>(si)[k] = gi[k];
-        __syncwarp(mask);
-        pdlWait(); // the writes start here
         int32_t const dEnd = a.grpOff[g + 1];
         constexpr int U = 4;
+        // the map of the next batch of positions is loaded while this one is summed and
+        // reduced; the first batch's loads are issued before the codes are staged
+        int32_t npos[U];
+        int nb0[U], nb1[U];
+        auto loadBatch = [&](int32_t d0) {
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+          {
+            int32_t const d = d0 + u * W + lane;
+            npos[u] = d < dEnd ? a.grpPos[d] : 0;
+            nb0[u] = d < dEnd ? a.grpBeg[d] : 0;
+            nb1[u] = d + 1 < dEnd ? a.grpBeg[d + 1] : nItems;
+          }
+        };
+        loadBatch(a.grpOff[g]);
+        // the group's codes: W * 100 of them, 16 bytes (8 codes) per load; the map pads
+        // the last group's codes to a multiple of 8
+        uint4 const * const gi = reinterpret_cast<uint4 const *>(a.grpItem + g * kP2GroupItems);
+        // every load of a batch in flight before the first store: at most 13 per lane
+        // for any warp width (ceil(12.5 W) / W < 13.5), in two batches of seven
+        int const n8 = (nItems + 7) / 8;
+        uint4 * const si4 = reinterpret_cast<uint4 *>(si);
+        static_assert(kP2GroupItems / 8 <= 32 * 14, "code staging batches");
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+          uint4 tmp[7];
+#pragma unroll
+          for (int r = 0; r < 7; ++r)
+          {
+            int const k = lane + (7 * h + r) * W;
+            if (k < n8)
+              tmp[r] = gi[k];
+          }
+#pragma unroll
+          for (int r = 0; r < 7; ++r)
+          {
+            int const k = lane + (7 * h + r) * W;
+            if (k < n8)
+              si4[k] = tmp[r];
+          }
+        }
+        __syncwarp(mask);
+        pdlWait(); // the writes start here
         for (int32_t d0 = a.grpOff[g]; d0 < dEnd; d0 += U * W)
         {
           int32_t pos[U];
           int b0[U], b1[U];
 #pragma unroll
           for (int u = 0; u < U; ++u)
-          {
-            int32_t const d = d0 + u * W + lane;
-            pos[u] = d < dEnd ? a.grpPos[d] : 0;
-            b0[u] = d < dEnd ? a.grpBeg[d] : 0;
-            b1[u] = d + 1 < dEnd ? a.grpBeg[d + 1] : nItems;
-          }
+            pos[u] = npos[u], b0[u] = nb0[u], b1[u] = nb1[u];
+          loadBatch(d0 + U * W);
 #pragma unroll
           for (int u = 0; u < U; ++u)
           {
