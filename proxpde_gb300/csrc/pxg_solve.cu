@@ -8,11 +8,18 @@
 //
 // CG design: every scalar (alpha, beta, r.z, residual, done flag, iteration count)
 // stays in device memory; dot products are reduced in two deterministic passes
-// (per-block partials, then one block); a chunk of iterations is captured once in a
-// CUDA graph and replayed, and the host reads the done flag once per chunk.  Kernels
-// after convergence return immediately, so a partly used chunk costs launches only.
+// (per-block partials, then a fixed-order sum that every block of the next kernel does
+// itself, so that an iteration is three kernels: the product, the update of x, r and z,
+// the update of p); a chunk of iterations is captured once in a CUDA graph and
+// replayed, and the host reads the done flag once per chunk.  Kernels after
+// convergence return immediately, so a partly used chunk costs launches only.
+// GB300's FP64 rate (1/64 of FP32) makes the product about as FP64-bound as it is
+// HBM-bound: every entry is one FMA, and every unused slot of a row's last round and
+// every shuffle addition costs a slot too, so the lanes per row and entries per lane
+// follow the matrix's mean row length.
 #include <cub/block/block_reduce.cuh>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -29,7 +36,7 @@ constexpr int kChunk = 16; // CG iterations per captured graph
 
 enum : int
 {
-  S_RZ = 0,
+  S_RZ = 0, // r.z of the iterations of even index (S_RZNEW: odd)
   S_PQ,
   S_RZNEW,
   S_RR,
@@ -131,6 +138,8 @@ __global__ void __launch_bounds__(kTpb) kFinalInit(double const * __restrict__ p
   s[S_DONE] = (t[1] == 0.) ? 1. : 0.;
 }
 
+// q = A p and the partials of p.q; LPR lanes per row, UNR entries per lane and round
+template <int LPR, int UNR>
 __global__ void __launch_bounds__(kTpb) kSpmvDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
                                                  double const * __restrict__ a, double const * __restrict__ p,
                                                  int64_t n, double * __restrict__ q, double * __restrict__ part,
@@ -139,16 +148,16 @@ __global__ void __launch_bounds__(kTpb) kSpmvDot(int32_t const * __restrict__ rp
   if (s[S_DONE] != 0.)
     return;
   double acc[1] = {0.};
-  constexpr int RPW = 32 / kLpr; // rows per warp step
+  constexpr int RPW = 32 / LPR; // rows per warp step
   int64_t const warps = (int64_t)gridDim.x * (blockDim.x / 32);
   int64_t const w = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   int const lane = threadIdx.x & 31;
   for (int64_t r0 = w * RPW; r0 < n; r0 += warps * RPW)
   {
-    int64_t const row = r0 + lane / kLpr;
+    int64_t const row = r0 + lane / LPR;
     bool const valid = row < n;
-    double const t = rowDot<false>(rp, ci, a, p, row, valid);
-    if (valid && (lane & (kLpr - 1)) == 0)
+    double const t = rowDot<false, LPR, UNR>(rp, ci, a, p, row, valid);
+    if (valid && (lane & (LPR - 1)) == 0)
     {
       q[row] = t;
       acc[0] += p[row] * t;
@@ -157,27 +166,27 @@ __global__ void __launch_bounds__(kTpb) kSpmvDot(int32_t const * __restrict__ rp
   blockSum<1>(acc, part + blockIdx.x);
 }
 
-__global__ void __launch_bounds__(kTpb) kFinalAlpha(double const * __restrict__ part, int nb, double * __restrict__ s)
-{
-  if (s[S_DONE] != 0.)
-    return;
-  double t[1];
-  sumPartials<1>(part, nb, t);
-  if (threadIdx.x != 0)
-    return;
-  s[S_PQ] = t[0];
-  s[S_ALPHA] = s[S_RZ] / t[0];
-}
+__device__ __forceinline__ int rzSlot(int parity) { return parity ? S_RZNEW : S_RZ; }
 
+// x += alpha p, r -= alpha q, z = D^-1 r and the partials of r.z and r.r, with
+// alpha = r.z / p.q from the product's partials (every block sums them in the same
+// order, so all use the same alpha); `parity` is the iteration index's
 __global__ void __launch_bounds__(kTpb) kCgUpdate(double * __restrict__ x, double * __restrict__ r,
                                                   double const * __restrict__ p, double const * __restrict__ q,
                                                   double const * __restrict__ dinv, double * __restrict__ z,
-                                                  int64_t n, double * __restrict__ part,
-                                                  double const * __restrict__ s)
+                                                  int64_t n, double const * __restrict__ partPQ, int nb,
+                                                  double * __restrict__ part, double * __restrict__ s, int parity)
 {
   if (s[S_DONE] != 0.)
     return;
-  double const al = s[S_ALPHA];
+  double pq[1];
+  sumPartials<1>(partPQ, nb, pq);
+  double const al = s[rzSlot(parity)] / pq[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+  {
+    s[S_PQ] = pq[0];
+    s[S_ALPHA] = al;
+  }
   double acc[2] = {0., 0.};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
   {
@@ -192,29 +201,34 @@ __global__ void __launch_bounds__(kTpb) kCgUpdate(double * __restrict__ x, doubl
   blockSum<2>(acc, part + 2 * blockIdx.x);
 }
 
-__global__ void __launch_bounds__(kTpb) kFinalBeta(double const * __restrict__ part, int nb, double * __restrict__ s)
+// p = z + beta p with beta = r.z (new) / r.z (old) from the update's partials (every
+// block sums them in the same order); block 0 stores the new r.z in the other parity's
+// slot, counts the iteration and raises the done flag.  The flag is read once per
+// block (a block that sees it raised by block 0 skips an update nobody reads).
+__global__ void __launch_bounds__(kTpb) kPUpdate(double * __restrict__ p, double const * __restrict__ z, int64_t n,
+                                                 double const * __restrict__ part, int nb, double * __restrict__ s,
+                                                 int parity)
 {
-  if (s[S_DONE] != 0.)
+  __shared__ int done;
+  if (threadIdx.x == 0)
+    done = s[S_DONE] != 0.;
+  __syncthreads();
+  if (done)
     return;
   double t[2];
   sumPartials<2>(part, nb, t);
-  if (threadIdx.x != 0)
-    return;
   double const rz = t[0], rr = t[1];
-  s[S_RR] = rr;
-  s[S_ITER] += 1.;
-  s[S_BETA] = rz / s[S_RZ];
-  s[S_RZ] = rz;
-  if (rr <= s[S_TOL2] * s[S_BB] || s[S_ITER] >= s[S_MAXIT] || !(rr == rr))
-    s[S_DONE] = 1.;
-}
-
-__global__ void __launch_bounds__(kTpb) kPUpdate(double * __restrict__ p, double const * __restrict__ z, int64_t n,
-                                                 double const * __restrict__ s)
-{
-  if (s[S_DONE] != 0.)
-    return;
-  double const be = s[S_BETA];
+  double const be = rz / s[rzSlot(parity)];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+  {
+    s[rzSlot(parity ^ 1)] = rz;
+    s[S_RR] = rr;
+    s[S_BETA] = be;
+    double const it = s[S_ITER] + 1.;
+    s[S_ITER] = it;
+    if (rr <= s[S_TOL2] * s[S_BB] || it >= s[S_MAXIT] || !(rr == rr))
+      s[S_DONE] = 1.;
+  }
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = z[i] + be * p[i];
 }
@@ -272,7 +286,7 @@ pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double c
     PXG_CUDA(c, w.p.alloc(n));
     PXG_CUDA(c, w.q.alloc(n));
     PXG_CUDA(c, w.dinv.alloc(n));
-    PXG_CUDA(c, w.part.alloc(2 * kMaxPartBlocks));
+    PXG_CUDA(c, w.part.alloc(3 * kMaxPartBlocks)); // p.q, then r.z and r.r
     PXG_CUDA(c, w.scal.alloc(S_COUNT));
     w.n = n;
   }
@@ -293,17 +307,34 @@ pxg_status cgSolve(pxg_ctx * c, int32_t const * rp, int32_t const * ci, double c
   kFinalInit<<<1, kTpb, 0, s>>>(w.part.p, nb, w.scal.p, rtol * rtol, (double)maxIter);
   PXG_CUDA(c, cudaGetLastError());
 
-  // capture one chunk of iterations
+  // the product's row split from the mean row length (P1 tetrahedra ~15, Q1 hexahedra
+  // ~27, longer rows several rounds of 32)
+  int32_t nnz = 0;
+  PXG_CUDA(c, cudaMemcpyAsync(&nnz, rp + n, sizeof(nnz), cudaMemcpyDeviceToHost, s));
+  PXG_CUDA(c, cudaStreamSynchronize(s));
+  double const meanRow = n > 0 ? (double)nnz / (double)n : 0.;
+  auto spmv = meanRow <= 16. ? kSpmvDot<2, 8> : meanRow <= 28. ? kSpmvDot<2, 14> : kSpmvDot<4, 8>;
+  // the product's grid: one wave of resident blocks (its register use limits them),
+  // so that no second, partial wave trails
+  int perSm = 0;
+  PXG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, spmv, kTpb, 0));
+  int64_t const rowsPerBlock = kTpb / 2;
+  int const nbS = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)kMaxPartBlocks, (int64_t)perSm * c->sms,
+                                                                (n + rowsPerBlock - 1) / rowsPerBlock}));
+  double * const partPQ = w.part.p;
+  double * const partRZ = w.part.p + kMaxPartBlocks;
+
+  // capture one chunk of iterations (an even number, so that the parity of an
+  // iteration's index is its position's in the chunk)
+  static_assert(kChunk % 2 == 0, "r.z slots alternate by iteration");
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   PXG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < kChunk; ++k)
   {
-    kSpmvDot<<<nb, kTpb, 0, s>>>(rp, ci, a, w.p.p, n, w.q.p, w.part.p, w.scal.p);
-    kFinalAlpha<<<1, kTpb, 0, s>>>(w.part.p, nb, w.scal.p);
-    kCgUpdate<<<nb, kTpb, 0, s>>>(x, w.r.p, w.p.p, w.q.p, w.dinv.p, w.z.p, n, w.part.p, w.scal.p);
-    kFinalBeta<<<1, kTpb, 0, s>>>(w.part.p, nb, w.scal.p);
-    kPUpdate<<<nb, kTpb, 0, s>>>(w.p.p, w.z.p, n, w.scal.p);
+    spmv<<<nbS, kTpb, 0, s>>>(rp, ci, a, w.p.p, n, w.q.p, partPQ, w.scal.p);
+    kCgUpdate<<<nb, kTpb, 0, s>>>(x, w.r.p, w.p.p, w.q.p, w.dinv.p, w.z.p, n, partPQ, nbS, partRZ, w.scal.p, k & 1);
+    kPUpdate<<<nb, kTpb, 0, s>>>(w.p.p, w.z.p, n, partRZ, nb, w.scal.p, k & 1);
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
   if (ce == cudaSuccess)
