@@ -374,23 +374,35 @@ __device__ void buildChunks(BatchDev const & d, int par)
   __threadfence();
 }
 
-// q = K p over the rows [c0, c0 + nr) of one chunk; returns the thread's share of p.q
+// q = K p over the rows [c0, c0 + nr) of one chunk; returns the thread's share of p.q.
+// A warp takes 32 rows at a time, LPR batches of 32 / LPR rows (LPR lanes per row), and
+// reduces the lane partials with transposeReduce, so that every lane ends with one
+// row's value: the FP64 pipe, which bounds this phase with the matrix stream, spends
+// LPR - 1 additions and one p.q FMA per lane on 32 rows instead of log2(LPR) additions
+// per batch and a p.q FMA that only one lane in LPR uses.
 template <int LPR, int UNR>
 __device__ __forceinline__ double spmvChunk(SysDev const & s, int64_t c0, int nr)
 {
   constexpr int RPW = 32 / LPR;
   int const lane = threadIdx.x & 31, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
+  int const sub = lane & (LPR - 1);
   double pq = 0.;
-  for (int v0 = warp * RPW; v0 < nr; v0 += nwarps * RPW)
+  for (int v0 = warp * 32; v0 < nr; v0 += nwarps * 32)
   {
-    int const v = v0 + lane / LPR;
-    bool const act = v < nr;
-    int64_t const lr = c0 + (act ? v : 0);
-    double const t = rowDot<true, LPR, UNR>(s.rp, s.ci, s.K, s.p, lr, act);
-    if (act && (lane & (LPR - 1)) == 0)
+    double t[LPR];
+#pragma unroll
+    for (int k = 0; k < LPR; ++k)
     {
-      __stcg(s.q + lr, t);
-      pq += __ldcg(s.p + lr) * t;
+      int const v = v0 + k * RPW + lane / LPR;
+      bool const act = v < nr;
+      t[k] = rowDot<true, LPR, UNR, false>(s.rp, s.ci, s.K, s.p, c0 + (act ? v : 0), act);
+    }
+    double const qv = transposeReduce<LPR>(t, sub);
+    int const v = v0 + sub * RPW + lane / LPR; // the row whose value this lane holds
+    if (v < nr)
+    {
+      __stcg(s.q + c0 + v, qv);
+      pq += __ldcg(s.p + c0 + v) * qv;
     }
   }
   return pq;

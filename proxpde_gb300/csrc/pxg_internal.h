@@ -543,7 +543,7 @@ constexpr int kUnr = 8;  // entries per lane and load round
 // issues every slot of a round, used or not (GB300: 1/64 of the FP32 rate), so LPR x
 // UNR should just cover the typical row: 4 x 7 for Q1 hexahedra (27 entries), 2 x 8
 // for P1 tetrahedra (15).
-template <bool L2ONLY, int LPR = kLpr, int UNR = kUnr>
+template <bool L2ONLY, int LPR = kLpr, int UNR = kUnr, bool REDUCE = true>
 __device__ __forceinline__ double rowDot(int32_t const * __restrict__ rp, int32_t const * __restrict__ ci,
                                          double const * __restrict__ a, double const * x, int64_t row, bool valid)
 {
@@ -575,10 +575,40 @@ __device__ __forceinline__ double rowDot(int32_t const * __restrict__ rp, int32_
           t = fma(av[u], L2ONLY ? __ldcg(x + cc[u]) : x[cc[u]], t);
     }
   }
+  if constexpr (REDUCE)
+  {
 #pragma unroll
-  for (int o = LPR / 2; o > 0; o >>= 1)
-    t += __shfl_xor_sync(0xffffffffu, t, o);
+    for (int o = LPR / 2; o > 0; o >>= 1)
+      t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
   return t;
+}
+
+// The lane partials t[k] of LPR rows (row k of the lane's group in the k-th of LPR
+// consecutive row batches), reduced so that the lane whose position in its group is
+// `sub` returns the whole sum of row `sub`: log2(LPR) halving stages, in each of which
+// a lane keeps the half of its rows its partner does not and adds the partner's share
+// of them.  LPR - 1 additions per lane for LPR rows, where the butterfly of rowDot
+// takes log2(LPR) per row; the lanes are paired as in that butterfly (xor LPR/2 first),
+// so every row sum is the same double.
+template <int LPR>
+__device__ __forceinline__ double transposeReduce(double (&t)[LPR], int sub)
+{
+  if constexpr (LPR == 1)
+    return t[0];
+  else
+  {
+    constexpr int H = LPR / 2;
+    bool const upper = (sub & H) != 0;
+    double keep[H];
+#pragma unroll
+    for (int k = 0; k < H; ++k)
+    {
+      double const send = upper ? t[k] : t[k + H];
+      keep[k] = (upper ? t[k + H] : t[k]) + __shfl_xor_sync(0xffffffffu, send, H);
+    }
+    return transposeReduce<H>(keep, sub);
+  }
 }
 } // namespace pxg
 
