@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "pxg_internal.h"
+#include "pxg_sinpi.h"
 
 namespace pxg
 {
@@ -43,7 +44,8 @@ constexpr int NQ = 27, N = 27, NP = N * (N + 1) / 2;
 // 3(3a + b) + k.  Symmetric classes: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2).
 __device__ double gCoef[72];
 __device__ double gCoefN[72];      // P, D, E classes divided by their first coefficient
-__device__ double gScale[3 * 216 + 3 * 486]; // deferred scale of every stiffness table value
+constexpr int kTab = 3 * 216 + 3 * 486;  // S_x S_y S_z U_xy U_xz U_yz
+__device__ double gScale[kTab];           // deferred scale of every stiffness table value
 __device__ double gT[3];           // t_k
 __device__ double gWl[NQ];         // weights in lattice order qx * 9 + qy * 3 + qz
 __device__ uint8_t gRuleOfLat[NQ]; // the rule's point index of each lattice point
@@ -56,7 +58,6 @@ __device__ uint16_t gPairsF[NP];   // (i << 8 | j), i <= j
 __device__ uint16_t gPairIdx[NP * 8];
 constexpr int kPairsPerLane = (NP + 31) / 32; // 12
 
-constexpr int kTab = 3 * 216 + 3 * 486; // S_x S_y S_z U_xy U_xz U_yz
 
 __host__ __device__ constexpr int symCls(int a, int b)
 {
@@ -277,8 +278,6 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
   __syncwarp();
   double const * const cL = S.coef;
   double const * const cP = S.coef + 9;
-  double const * const cD = S.coef + 27;
-  double const * const cE = S.coef + 45;
 
   // ---- load vector (buildLhs' BC values, buildRhs); the writes start here
   pdlWait();
@@ -298,7 +297,9 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
     if (lane < NQ)
     {
       double f;
-      if (a.rkind == 1)
+      if (a.rkind == 1 && a.fn == PXG_FN_SIN3)
+        f = rc * (sinPiTab(S.scr[0][lane]) * sinPiTab(S.scr[0][32 + lane]) * sinPiTab(S.scr[0][64 + lane]));
+      else if (a.rkind == 1)
         f = evalPoint(a.fn, rc, S.scr[0][lane], S.scr[0][32 + lane], S.scr[0][64 + lane]);
       else if (a.rkind == 3)
         f = rc * a.field[e * NQ + S.ruleOfLat[lane]];
