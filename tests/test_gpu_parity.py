@@ -118,6 +118,38 @@ def test_bc_lift_and_projection(engine, t, gen):
     assert_close(g["b"], b, what="rhs with lift")
 
 
+def test_p2_group_scatter_overwrites_and_accumulates(engine):
+    """The P2 warp-group scatter on outputs holding other values: an overwriting call
+    matches the oracle, and an accumulating second call doubles K and M (to round-off
+    of the reductions' order)."""
+    import torch
+
+    from proxpde_gb300 import Context
+
+    xyz, conn, k = problem("tet6", 3, 0.15, seed=5, sigma=0.5)  # 162 elements: a partial last warp
+    ctx = Context(0)
+    ctx.set_mesh(O.P2TET, xyz, conn)
+    ndof = ctx.build_dofmap()
+    nnz = ctx.build_pattern()
+    ctx.set_coef(k)
+    K = torch.full((nnz,), 7.0, dtype=torch.float64, device="cuda")  # overwritten, not added to
+    M = torch.full_like(K, -3.0)
+    ctx.assemble(op0=K_OP, vals0=K, op1=M_OP, vals1=M)
+    K1, M1 = K.clone(), M.clone()
+    import scipy.sparse as sp
+
+    em, _ = O.dofmap(O.P2TET, xyz.shape[0], conn)
+    rp, ci = ctx.get_pattern()
+    for op, v in ((K_OP, K1), (M_OP, M1)):
+        csr, _ = O.build(O.P2TET, xyz, conn, em, ndof, lhs=oracle_lhs(op, k), nthreads=4)
+        A = sp.csr_matrix((v.cpu().numpy(), ci, rp), shape=(ndof, ndof))
+        B = sp.csr_matrix((csr[2], csr[1], csr[0]), shape=(ndof, ndof))
+        assert abs(A - B).max() <= 1e-12 * abs(B).max()
+    ctx.assemble(op0=K_OP, vals0=K, op1=M_OP, vals1=M, accumulate=True)
+    for v, v1 in ((K, K1), (M, M1)):
+        assert float((v - 2 * v1).abs().max()) <= 1e-14 * float(v1.abs().max())
+
+
 def test_accumulate_and_single_element(engine):
     import torch
 
