@@ -358,7 +358,9 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
       d22[p][t] = fma(c2[p][t][0], c2[p][t][0], fma(c2[p][t][1], c2[p][t][1], c2[p][t][2] * c2[p][t][2]));
       d33[p][t] = fma(c3[p][t][0], c3[p][t][0], fma(c3[p][t][1], c3[p][t][1], c3[p][t][2] * c3[p][t][2]));
     }
-  double G[6][8]; // xx yy zz xy xz yz of k |det J| (J^T J)^-1, x8
+  // xx yy zz xy xz yz of k |det J| (J^T J)^-1, x8; the diagonal three unscaled, their
+  // scale sG folded into the first contraction of their tables
+  double G[6][8], sG[8];
   double ad[8];   // |det J|, x512
   double u[8][3]; // J xi / (g / 8): the qpoint offset
 #pragma unroll
@@ -382,7 +384,7 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
     double const rs = rsqrtN(D);
     ad[q] = D * rs;
     double const s = kk * rs;
-    G[0][q] = s * A11, G[1][q] = s * A22, G[2][q] = s * A33;
+    G[0][q] = A11, G[1][q] = A22, G[2][q] = A33, sG[q] = s;
     G[3][q] = s * A12, G[4][q] = s * A13, G[5][q] = s * A23;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -595,7 +597,8 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
       for (int z = 0; z < 2; ++z)
       {
         double w[3];
-        cW3(G[0][4 * z] + G[0][1 + 4 * z], G[0][2 + 4 * z] + G[0][3 + 4 * z], w);
+        cW3(fma(sG[4 * z], G[0][4 * z], sG[1 + 4 * z] * G[0][1 + 4 * z]),
+            fma(sG[2 + 4 * z], G[0][2 + 4 * z], sG[3 + 4 * z] * G[0][3 + 4 * z]), w);
         R[0][z] = w[0], R[1][z] = w[1], R[2][z] = w[2];
       }
 #pragma unroll
@@ -609,7 +612,8 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
       for (int z = 0; z < 2; ++z)
       {
         double w[3];
-        cW3(G[1][4 * z] + G[1][2 + 4 * z], G[1][1 + 4 * z] + G[1][3 + 4 * z], w);
+        cW3(fma(sG[4 * z], G[1][4 * z], sG[2 + 4 * z] * G[1][2 + 4 * z]),
+            fma(sG[1 + 4 * z], G[1][1 + 4 * z], sG[3 + 4 * z] * G[1][3 + 4 * z]), w);
         R[0][z] = w[0], R[1][z] = w[1], R[2][z] = w[2];
       }
 #pragma unroll
@@ -623,7 +627,8 @@ __global__ void __launch_bounds__(NT, MINB) kAssembleQ1F64(AsmArgs a)
       for (int y = 0; y < 2; ++y)
       {
         double w[3];
-        cW3(G[2][2 * y] + G[2][2 * y + 4], G[2][1 + 2 * y] + G[2][1 + 2 * y + 4], w);
+        cW3(fma(sG[2 * y], G[2][2 * y], sG[2 * y + 4] * G[2][2 * y + 4]),
+            fma(sG[1 + 2 * y], G[2][1 + 2 * y], sG[1 + 2 * y + 4] * G[2][1 + 2 * y + 4]), w);
         R[0][y] = w[0], R[1][y] = w[1], R[2][y] = w[2];
       }
 #pragma unroll
