@@ -15,13 +15,19 @@
 //    reference's J), J^T J, its adjugate and determinant D, 1/|det J| = rsqrt(D) (one
 //    third-order Newton step), w_q |det J_q|, G_q = k w_q |det J| (J^T J)^-1;
 //  - stiffness tables, each three one-axis contractions of one G component with the
-//    1D products D_ab = l'_a l'_b, P_ab = l_a l_b (6 symmetric classes) or
-//    E_ab = l'_a l_b (9): S_x = sum G_xx D P P, S_y, S_z (216 values each) and
-//    U_xy = sum G_xy E E P, U_xz, U_yz (486 each), the 6-class axis contracted first;
+//    1D products D_ab = l'_a l'_b, P_ab = l_a l_b (6 symmetric classes): S_x = sum
+//    G_xx D P P, S_y, S_z (216 values each).  The mixed terms of K_ij,
+//    sum G_xy (E_ix,jx E_jy,iy + E_jx,ix E_iy,jy) P with E_ab = l'_a l_b, split E into
+//    its symmetric part S_ab = (l_a l_b)'/2 (6 classes) and antisymmetric part
+//    A_ab = (l'_a l_b - l'_b l_a)/2 (3 classes, a < b, and its sign): the sum is
+//    2 sum G S S P - 2 s_x s_y sum G A A P, so each of G_xy, G_xz, G_yz gives a table SS
+//    (216 values) and a table AA (54), sharing their first stage (the 6-class P axis),
+//    instead of the 486 values of sum G E E P;
 //    the stiffness stages use each class's three coefficients divided by the first, so
 //    that an output costs two FP64 operations, and an entry K_ij, a sum of nine table
-//    values (three S, two of each U), multiplies each by its deferred scale (the
-//    product of the three classes' first coefficients) in the FMA that adds it;
+//    values (three S, an SS and an AA per mixed component), multiplies each by its
+//    deferred scale (the product of the three classes' first coefficients, with the
+//    factor 2 and the sign) in the FMA that adds it;
 //  - mass table sum |det J| w P P P (216), M_ij one value of it;
 //  - the load r_q = w_q |det J_q| f(qpoint_q), contracted to the nodes with l_a.
 // About 16k FP64 operations per element against about 100k for the per-point form.
@@ -40,12 +46,17 @@ namespace q2f
 constexpr int NQ = 27, N = 27, NP = N * (N + 1) / 2;
 
 // 1D tables at the three Gauss points t_0 < t_1 = 0 < t_2 (from initQ2F64Tables):
-// [0, 9) l_a(t_k) at 3a + k; [9, 27) P classes; [27, 45) D classes; [45, 72) E_ab at
-// 3(3a + b) + k.  Symmetric classes: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2).
+// [0, 9) l_a(t_k) at 3a + k; [9, 27) P classes; [27, 45) D classes; [45, 63) S classes;
+// [63, 72) A classes.  Symmetric classes: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2);
+// antisymmetric: (0,1) (0,2) (1,2).
 __device__ double gCoef[72];
-__device__ double gCoefN[72];      // P, D, E classes divided by their first coefficient
-constexpr int kTab = 3 * 216 + 3 * 486;  // S_x S_y S_z U_xy U_xz U_yz
-__device__ double gScale[kTab];           // deferred scale of every stiffness table value
+__device__ double gCoefN[72];      // P, D, S, A classes divided by their first coefficient
+// the deferred scales: S_x S_y S_z (216 each), then per mixed component its SS table
+// (216) and its AA table (128: index a for a positive orientation, 64 + a for a
+// negative one, 54 for the pairs without an AA term, whose scale is 0)
+constexpr int kAA = 128;
+constexpr int kTab = 3 * 216 + 3 * (216 + kAA);
+__device__ double gScale[kTab];
 __device__ double gT[3];           // t_k
 __device__ double gWl[NQ];         // weights in lattice order qx * 9 + qy * 3 + qz
 __device__ uint8_t gRuleOfLat[NQ]; // the rule's point index of each lattice point
@@ -53,8 +64,9 @@ __device__ uint8_t gLatOfNode[N];  // node n -> ax * 9 + ay * 3 + az (1D functio
 __device__ uint8_t gNodeOfLat[N];
 __device__ uint16_t gPairsF[NP];   // (i << 8 | j), i <= j
 // per pair, its index into each table (the layouts of the contractions below): the S
-// tables' (shared by the mass and S_x, S_y, S_z), then U_xy, U_xy transposed, U_xz,
-// U_xz transposed, U_yz, U_yz transposed; 8 per pair (one padding)
+// tables' (shared by the mass and S_x, S_y, S_z), then SS_xy, AA_xy, SS_xz, AA_xz,
+// SS_yz, AA_yz (an AA index with the orientation, as gScale lays them out); 8 per pair
+// (one padding)
 __device__ uint16_t gPairIdx[NP * 8];
 constexpr int kPairsPerLane = (NP + 31) / 32; // 12
 
@@ -152,7 +164,8 @@ struct Smem
   double H[8][3]; // Walsh-Hadamard transform of the vertices, [kx + 2 ky + 4 kz][r]
   double G[6][NQ];
   double ad[NQ];
-  double tab[486]; // one table at a time: the mass, then S_x, S_y, S_z, U_xy, U_xz, U_yz
+  double tab[272]; // one table at a time: the mass, S_x, S_y, S_z, then SS [0, 216) and
+                   // AA [216, 270) of each mixed component, tab[270] = 0
   double scr[2][243];
   double bv[N];
   uint32_t dof[N];
@@ -355,8 +368,9 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
         kv[k] = fma(S.tab[t0], __ldg(gScale + scaleBase + t0), kv[k]);
         if (slot1 >= 0)
         {
+          // the AA value of the pair's orientation (index mod 64) and its signed scale
           int const t1 = gPairIdx[8 * p + slot1];
-          kv[k] = fma(S.tab[t1], __ldg(gScale + scaleBase + t1), kv[k]);
+          kv[k] = fma(S.tab[216 + (t1 & 63)], __ldg(gScale + scaleBase + 216 + t1), kv[k]);
         }
       }
     }
@@ -375,19 +389,30 @@ __global__ void __launch_bounds__(32) kAssembleQ2F64(AsmArgs a)
   {
     double const * const nP = S.coefN + 9;
     double const * const nD = S.coefN + 27;
-    double const * const nE = S.coefN + 45;
+    double const * const nS = S.coefN + 45;
+    double const * const nA = S.coefN + 63;
     contract3N(S.G[0], 6, nD, 6, nP, 6, nP, S.tab, S.scr[0], S.scr[1], lane); // [px][py][pz]
     addTable(0, -1, 0, false);
     contract3N(S.G[1], 6, nP, 6, nD, 6, nP, S.tab, S.scr[0], S.scr[1], lane);
     addTable(0, -1, 216, false);
     contract3N(S.G[2], 6, nP, 6, nP, 6, nD, S.tab, S.scr[0], S.scr[1], lane);
     addTable(0, -1, 432, false);
-    contract3N(S.G[3], 6, nP, 9, nE, 9, nE, S.tab, S.scr[0], S.scr[1], lane); // [pz][ex][ey]
+    // a mixed component: SS into tab[0, 216), then AA from the same first stage (scr[0])
+    // into tab[216, 270), and the zero that pairs without an AA term read
+    auto mixed = [&](double const * g) {
+      contract3N(g, 6, nP, 6, nS, 6, nS, S.tab, S.scr[0], S.scr[1], lane);
+      stageN(S.scr[0], 18, 3, nA, S.scr[1], lane);
+      stageN(S.scr[1], 18, 3, nA, S.tab + 216, lane);
+      if (lane == 0)
+        S.tab[270] = 0.;
+      __syncwarp();
+    };
+    mixed(S.G[3]); // [pz][sx][sy], [pz][ax][ay]
     addTable(1, 2, 648, false);
-    contract3N(S.G[4], 6, nP, 9, nE, 9, nE, S.tab, S.scr[0], S.scr[1], lane); // [py][ex][ez]
-    addTable(3, 4, 1134, false);
-    contract3N(S.G[5], 6, nP, 9, nE, 9, nE, S.tab, S.scr[0], S.scr[1], lane); // [px][ey][ez]
-    addTable(5, 6, 1620, false);
+    mixed(S.G[4]); // [py][sx][sz], [py][ax][az]
+    addTable(3, 4, 648 + (216 + kAA), false);
+    mixed(S.G[5]); // [px][sy][sz], [px][ay][az]
+    addTable(5, 6, 648 + 2 * (216 + kAA), false);
   }
 
   // ---- the scatter of the entries i <= j
@@ -470,10 +495,19 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
       coef[9 + 3 * cc + k] = f(cls[cc][0], t[k]) * f(cls[cc][1], t[k]);
       coef[27 + 3 * cc + k] = df(cls[cc][0], t[k]) * df(cls[cc][1], t[k]);
     }
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b)
-      for (int k = 0; k < 3; ++k)
-        coef[45 + 3 * (3 * a + b) + k] = df(a, t[k]) * f(b, t[k]);
+  int const anti[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int cc = 0; cc < 6; ++cc)
+    for (int k = 0; k < 3; ++k)
+    {
+      int const a = cls[cc][0], b = cls[cc][1];
+      coef[45 + 3 * cc + k] = 0.5 * (df(a, t[k]) * f(b, t[k]) + df(b, t[k]) * f(a, t[k]));
+    }
+  for (int cc = 0; cc < 3; ++cc)
+    for (int k = 0; k < 3; ++k)
+    {
+      int const a = anti[cc][0], b = anti[cc][1];
+      coef[63 + 3 * cc + k] = 0.5 * (df(a, t[k]) * f(b, t[k]) - df(b, t[k]) * f(a, t[k]));
+    }
   // node n -> the 1D functions of its three factors: the lattice point where phi_n = 1
   uint8_t latOfNode[N], nodeOfLat[N];
   double const node1d[3] = {-1., 1., 0.};
@@ -495,7 +529,7 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
   for (int i = 0; i < N; ++i)
     for (int j = i; j < N; ++j)
       pairs.push_back((uint16_t)(i << 8 | j));
-  // the P, D, E classes divided by their first coefficient (the value at t_0, nonzero
+  // the P, D, S, A classes divided by their first coefficient (the value at t_0, nonzero
   // for every class), and the deferred scale of each stiffness table value: the
   // product of its three classes' first coefficients, in the tables' layouts
   std::vector<double> coefN(coef);
@@ -503,17 +537,18 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
   for (int k = 9; k < 72; k += 3)
     if (coef[k] == 0.)
       return fail(c, PXG_ERR_UNSUPPORTED, "Q2 tables: a class vanishes at the first Gauss point");
-  for (int base : {9, 27})
+  for (int base : {9, 27, 45})
     for (int cc = 0; cc < 6; ++cc)
       for (int k = 0; k < 3; ++k)
         coefN[base + 3 * cc + k] = coef[base + 3 * cc + k] / first(base, cc);
-  for (int cc = 0; cc < 9; ++cc)
+  for (int cc = 0; cc < 3; ++cc)
     for (int k = 0; k < 3; ++k)
-      coefN[45 + 3 * cc + k] = coef[45 + 3 * cc + k] / first(45, cc);
-  std::vector<double> scale(3 * 216 + 3 * 486);
+      coefN[63 + 3 * cc + k] = coef[63 + 3 * cc + k] / first(63, cc);
+  std::vector<double> scale(kTab, 0.);
   auto sP = [&](int cc) { return first(9, cc); };
   auto sD = [&](int cc) { return first(27, cc); };
-  auto sE = [&](int cc) { return first(45, cc); };
+  auto sS = [&](int cc) { return first(45, cc); };
+  auto sA = [&](int cc) { return first(63, cc); };
   for (int x = 0; x < 6; ++x)
     for (int y = 0; y < 6; ++y)
       for (int z = 0; z < 6; ++z)
@@ -523,14 +558,25 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
         scale[216 + k] = sP(x) * sD(y) * sP(z);
         scale[432 + k] = sP(x) * sP(y) * sD(z);
       }
-  for (int p = 0; p < 6; ++p)
-    for (int e1 = 0; e1 < 9; ++e1)
-      for (int e2 = 0; e2 < 9; ++e2)
-      {
-        double const v = sP(p) * sE(e1) * sE(e2);
-        for (int tbl = 0; tbl < 3; ++tbl)
-          scale[648 + 486 * tbl + p * 81 + e1 * 9 + e2] = v;
-      }
+  // mixed component m: 2 x SS, and -2 x orientation x AA (index 64 + a: the negative
+  // orientation; 54: no AA term, scale 0)
+  for (int m = 0; m < 3; ++m)
+  {
+    int const base = 648 + m * (216 + kAA);
+    for (int p = 0; p < 6; ++p)
+    {
+      for (int s1 = 0; s1 < 6; ++s1)
+        for (int s2 = 0; s2 < 6; ++s2)
+          scale[base + p * 36 + s1 * 6 + s2] = 2. * sP(p) * sS(s1) * sS(s2);
+      for (int a1 = 0; a1 < 3; ++a1)
+        for (int a2 = 0; a2 < 3; ++a2)
+        {
+          double const v = 2. * sP(p) * sA(a1) * sA(a2);
+          scale[base + 216 + p * 9 + a1 * 3 + a2] = -v;
+          scale[base + 216 + 64 + p * 9 + a1 * 3 + a2] = v;
+        }
+    }
+  }
   PXG_CUDA(c, cudaMemcpyToSymbol(gCoef, coef.data(), 72 * 8));
   PXG_CUDA(c, cudaMemcpyToSymbol(gCoefN, coefN.data(), 72 * 8));
   PXG_CUDA(c, cudaMemcpyToSymbol(gScale, scale.data(), scale.size() * 8));
@@ -540,10 +586,19 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
   PXG_CUDA(c, cudaMemcpyToSymbol(gLatOfNode, latOfNode, N));
   PXG_CUDA(c, cudaMemcpyToSymbol(gNodeOfLat, nodeOfLat, N));
   PXG_CUDA(c, cudaMemcpyToSymbol(gPairsF, pairs.data(), pairs.size() * 2));
-  // each pair's index into the tables: S (and mass) [px][py][pz]; U_xy [pz][ex][ey],
-  // U_xz [py][ex][ez], U_yz [px][ey][ez] with E classes 3a + b of l'_a l_b (the
-  // derivative's axis first), and their transposed terms
+  // each pair's index into the tables: S (and mass) [px][py][pz]; for the mixed
+  // components xy, xz, yz the SS tables [pz][sx][sy], [py][sx][sz], [px][sy][sz] (the
+  // symmetric classes of the two derivative axes) and the AA tables [pz][ax][ay], ... with
+  // the antisymmetric class a + b - 1 of {a, b}, plus 64 when the orientation
+  // sign(j_1 - i_1) sign(j_2 - i_2) is negative, and 54 when either axis pair is
+  // diagonal (no AA term)
   std::vector<uint16_t> pidx(pairs.size() * 8, 0);
+  auto aaIdx = [](int lead, int i1, int j1, int i2, int j2) -> uint16_t {
+    if (i1 == j1 || i2 == j2)
+      return 54;
+    int const v = lead * 9 + (i1 + j1 - 1) * 3 + (i2 + j2 - 1);
+    return (uint16_t)(((i1 < j1) == (i2 < j2)) ? v : 64 + v);
+  };
   for (size_t q = 0; q < pairs.size(); ++q)
   {
     int const i = pairs[q] >> 8, j = pairs[q] & 0xff;
@@ -552,12 +607,12 @@ pxg_status initQ2F64Tables(pxg_ctx * c)
     int const px = symCls(ix, jx), py = symCls(iy, jy), pz = symCls(iz, jz);
     uint16_t * const o = &pidx[8 * q];
     o[0] = (uint16_t)(px * 36 + py * 6 + pz);
-    o[1] = (uint16_t)(pz * 81 + (3 * ix + jx) * 9 + (3 * jy + iy));
-    o[2] = (uint16_t)(pz * 81 + (3 * jx + ix) * 9 + (3 * iy + jy));
-    o[3] = (uint16_t)(py * 81 + (3 * ix + jx) * 9 + (3 * jz + iz));
-    o[4] = (uint16_t)(py * 81 + (3 * jx + ix) * 9 + (3 * iz + jz));
-    o[5] = (uint16_t)(px * 81 + (3 * iy + jy) * 9 + (3 * jz + iz));
-    o[6] = (uint16_t)(px * 81 + (3 * jy + iy) * 9 + (3 * iz + jz));
+    o[1] = (uint16_t)(pz * 36 + px * 6 + py);
+    o[2] = aaIdx(pz, ix, jx, iy, jy);
+    o[3] = (uint16_t)(py * 36 + px * 6 + pz);
+    o[4] = aaIdx(py, ix, jx, iz, jz);
+    o[5] = (uint16_t)(px * 36 + py * 6 + pz);
+    o[6] = aaIdx(px, iy, jy, iz, jz);
   }
   PXG_CUDA(c, cudaMemcpyToSymbol(gPairIdx, pidx.data(), pidx.size() * 2));
   return PXG_OK;
