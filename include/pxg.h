@@ -338,7 +338,10 @@ pxg_status pxg_memcpy(pxg_ctx * ctx, void * dst, const void * src, uint64_t byte
  * x = A^-1 b to ||b - A x|| <= rtol ||b|| within max_iter iterations, x starting at 0.
  * proxpde solves with UmfPackLU (include/sparse_matrix.hpp:44, include/solver.hpp:65);
  * this plain device CG is the engine's solver.  Returns PXG_ERR_NOT_CONVERGED (x holds
- * the last iterate) when the tolerance is not met. */
+ * the last iterate) when the tolerance is not met.  The solve runs on a stream of the
+ * context ordered after `stream`, replays its iterations as a CUDA graph and reads its
+ * convergence flag on the host, so it returns with the solve complete and cannot be
+ * captured into the caller's graph. */
 pxg_status pxg_cg(pxg_ctx * ctx, const int32_t * row_ptr, const int32_t * col_idx,
                   const double * vals, int64_t n, const double * b, double * x, double rtol,
                   int max_iter, int * iters, double * rel_res, void * stream);
